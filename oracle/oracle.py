@@ -1,0 +1,268 @@
+"""ctypes loader for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module: it is the checker for the CUDA path, never part of it.
+
+Two libraries are exposed with the same Python surface:
+  * ``Oracle("port")``      -- oracle/euler2d_oracle.c, the C restatement of
+                               the reference CPU solver (builds anywhere);
+  * ``Oracle("reference")`` -- oracle/_ref/libref_euler2d.so, the unmodified
+                               reference sources behind ref_harness.cpp
+                               (only where the reference tree was present at
+                               build time; transmissive boundaries only).
+Grids are numpy float64 arrays of shape (ny+4, nx+4, 4): the Grid2D AoS
+layout of head/cpu/grid_cpu.hpp:10-89.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "liboracle_euler2d.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_euler2d.so")
+REFERENCE_TREE = "/root/reference"
+
+SOLVERS = {"hll": 0, "hllc": 1, "exact": 2, "force": 3}
+BC = {"transmissive": 0, "reflective": 1}
+
+_dp = C.POINTER(C.c_double)
+_llp = C.POINTER(C.c_longlong)
+
+
+class OrcGrid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int),
+                ("x_min", C.c_double), ("x_max", C.c_double),
+                ("y_min", C.c_double), ("y_max", C.c_double),
+                ("bc", C.c_int * 4)]
+
+
+def build(reference: bool | None = None) -> None:
+    """Compile the restatement (always) and the reference harness (when the
+    reference tree exists or ``reference`` is True)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    want_ref = os.path.isdir(REFERENCE_TREE) if reference is None else reference
+    if want_ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True,
+                       stderr=subprocess.DEVNULL)
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+class Grid:
+    """Geometry of one grid: interior nx x ny, 2 ghost layers, extents, BCs
+    (left, right, bottom, top)."""
+
+    def __init__(self, nx, ny, x_min=0.0, x_max=1.0, y_min=0.0, y_max=1.0,
+                 bc=("transmissive",) * 4):
+        self.nx, self.ny = int(nx), int(ny)
+        self.x_min, self.x_max, self.y_min, self.y_max = map(float, (x_min, x_max, y_min, y_max))
+        self.bc = tuple(bc)
+
+    @property
+    def shape(self):
+        return (self.ny + 4, self.nx + 4, 4)
+
+    def zeros(self):
+        return np.zeros(self.shape, dtype=np.float64)
+
+    def c(self) -> OrcGrid:
+        g = OrcGrid(self.nx, self.ny, self.x_min, self.x_max, self.y_min, self.y_max)
+        for k, b in enumerate(self.bc):
+            g.bc[k] = BC[b] if isinstance(b, str) else int(b)
+        return g
+
+    def ext(self):
+        return (self.nx, self.ny, self.x_min, self.x_max, self.y_min, self.y_max)
+
+    @property
+    def all_transmissive(self):
+        return all((b == "transmissive" or b == 0) for b in self.bc)
+
+
+class Oracle:
+    def __init__(self, kind: str = "port"):
+        self.kind = kind
+        path = PORT_SO if kind == "port" else REF_SO
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"oracle library missing: {path} (run oracle.build())")
+        self.lib = C.CDLL(path)
+        L = self.lib
+        if kind == "port":
+            G = C.POINTER(OrcGrid)
+            L.orc_apply_boundary.argtypes = [_dp, G]
+            L.orc_compute_dt.argtypes = [_dp, G, C.c_double, _dp]
+            L.orc_compute_dt.restype = C.c_int
+            L.orc_advance_second_order.argtypes = [_dp, _dp, _dp, G, C.c_double, C.c_int, _dp, _dp]
+            L.orc_advance_first_order.argtypes = [_dp, _dp, G, C.c_double, C.c_int]
+            L.orc_riemann_flux.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp]
+            L.orc_run.argtypes = [_dp, G, C.c_double, C.c_double, C.c_int, C.c_longlong, C.c_int,
+                                  _dp, _llp, _dp, C.c_longlong, _llp, _dp, _dp]
+            L.orc_run.restype = C.c_int
+            L.orc_init_blast.argtypes = [_dp, G] + [C.c_double] * 7
+            L.orc_init_shock_bubble.argtypes = [_dp, G] + [C.c_double] * 8
+            L.orc_init_reference_case.argtypes = [_dp, G, C.c_int]
+            L.orc_set_threads.argtypes = [C.c_int]
+            L.orc_get_threads.restype = C.c_int
+        else:
+            E = [C.c_int, C.c_int] + [C.c_double] * 4
+            L.ref_apply_transmissive_boundary.argtypes = [_dp] + E
+            L.ref_compute_dt.argtypes = [_dp] + E + [C.c_double, _dp]
+            L.ref_compute_dt.restype = C.c_int
+            L.ref_advance_second_order.argtypes = [_dp, _dp, _dp] + E + [C.c_double, C.c_int]
+            L.ref_advance_first_order.argtypes = [_dp, _dp] + E + [C.c_double, C.c_int]
+            L.ref_riemann_flux.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp]
+            L.ref_case_config.argtypes = [C.c_int, C.c_int, _dp]
+            L.ref_init_case.argtypes = [C.c_int, C.c_int, _dp]
+            L.ref_run.argtypes = [_dp] + E + [C.c_double, C.c_double, C.c_int, C.c_longlong,
+                                              C.c_int, _dp, _llp, _dp, C.c_longlong, _llp, _dp]
+            L.ref_run.restype = C.c_int
+
+    # -- helpers ---------------------------------------------------------
+    def _check_ref_grid(self, g: Grid):
+        if self.kind != "port" and not g.all_transmissive:
+            raise ValueError("the reference build only has transmissive boundaries")
+
+    def set_threads(self, n: int):
+        if self.kind == "port":
+            self.lib.orc_set_threads(int(n))
+        else:
+            os.environ["OMP_NUM_THREADS"] = str(n)
+
+    def threads(self) -> int:
+        if self.kind == "port":
+            return int(self.lib.orc_get_threads())
+        return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+    # -- API ---------------------------------------------------------------
+    def apply_boundary(self, U: np.ndarray, g: Grid) -> None:
+        assert U.flags.c_contiguous and U.dtype == np.float64 and U.shape == g.shape
+        if self.kind == "port":
+            gc = g.c()
+            self.lib.orc_apply_boundary(_p(U), C.byref(gc))
+        else:
+            self._check_ref_grid(g)
+            self.lib.ref_apply_transmissive_boundary(_p(U), *g.ext())
+
+    def compute_dt(self, U: np.ndarray, g: Grid, cfl: float):
+        dt = C.c_double(0.0)
+        if self.kind == "port":
+            gc = g.c()
+            rc = self.lib.orc_compute_dt(_p(U), C.byref(gc), cfl, C.byref(dt))
+        else:
+            rc = self.lib.ref_compute_dt(_p(U), *g.ext(), cfl, C.byref(dt))
+        if rc:
+            raise RuntimeError("compute_dt: non-positive maximum wave speed.")
+        return dt.value
+
+    def advance_second_order(self, Uold, g: Grid, dt: float, solver="hll", Utmp=None, Unew=None):
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        Utmp = g.zeros() if Utmp is None else Utmp
+        Unew = g.zeros() if Unew is None else Unew
+        Uold = np.ascontiguousarray(Uold, dtype=np.float64)
+        if self.kind == "port":
+            gc = g.c()
+            self.lib.orc_advance_second_order(_p(Uold), _p(Utmp), _p(Unew), C.byref(gc), dt, s,
+                                              None, None)
+        else:
+            self._check_ref_grid(g)
+            self.lib.ref_advance_second_order(_p(Uold), _p(Utmp), _p(Unew), *g.ext(), dt, s)
+        return Utmp, Unew
+
+    def advance_first_order(self, Uold, g: Grid, dt: float, solver="hll"):
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        Unew = g.zeros()
+        Uold = np.ascontiguousarray(Uold, dtype=np.float64)
+        if self.kind == "port":
+            gc = g.c()
+            self.lib.orc_advance_first_order(_p(Uold), _p(Unew), C.byref(gc), dt, s)
+        else:
+            self._check_ref_grid(g)
+            self.lib.ref_advance_first_order(_p(Uold), _p(Unew), *g.ext(), dt, s)
+        return Unew
+
+    def riemann_flux(self, UL, UR, direction: int, solver="hll"):
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        UL = np.ascontiguousarray(UL, dtype=np.float64)
+        UR = np.ascontiguousarray(UR, dtype=np.float64)
+        F = np.zeros(4)
+        fn = self.lib.orc_riemann_flux if self.kind == "port" else self.lib.ref_riemann_flux
+        fn(_p(UL), _p(UR), int(direction), s, _p(F))
+        return F
+
+    def run(self, U, g: Grid, cfl: float, t_end: float, solver="hll", max_steps=0, nsnap=0,
+            dt_cap=1 << 20, want_snapshots=False):
+        """Time loop of scripts/cpu/main_cpu.cpp:206-262.  U is advanced in place.
+        Returns dict(t, steps, dts, snap_step, snap_t[, snapshots])."""
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        t = C.c_double(0.0)
+        n = C.c_longlong(0)
+        cap = int(dt_cap) if max_steps <= 0 else min(int(dt_cap), int(max_steps))
+        dts = np.zeros(max(cap, 1))
+        ss = np.zeros(max(nsnap, 1), dtype=np.int64)
+        st = np.zeros(max(nsnap, 1))
+        snaps = None
+        if self.kind == "port":
+            gc = g.c()
+            if want_snapshots and nsnap > 0:
+                snaps = np.zeros((nsnap,) + g.shape)
+            rc = self.lib.orc_run(_p(U), C.byref(gc), cfl, t_end, s, int(max_steps), int(nsnap),
+                                  C.byref(t), C.byref(n), _p(dts), cap,
+                                  ss.ctypes.data_as(_llp), _p(st),
+                                  _p(snaps) if snaps is not None else None)
+        else:
+            self._check_ref_grid(g)
+            rc = self.lib.ref_run(_p(U), *g.ext(), cfl, t_end, s, int(max_steps), int(nsnap),
+                                  C.byref(t), C.byref(n), _p(dts), cap,
+                                  ss.ctypes.data_as(_llp), _p(st))
+        if rc:
+            raise RuntimeError("compute_dt: non-positive maximum wave speed.")
+        out = dict(t=t.value, steps=n.value, dts=dts[: min(n.value, cap)].copy(),
+                   snap_step=ss[:nsnap].copy(), snap_t=st[:nsnap].copy())
+        if snaps is not None:
+            out["snapshots"] = snaps
+        return out
+
+    # -- initial states (port only) ---------------------------------------
+    def init_blast(self, g: Grid, cx=1.0, cy=1.0, r=0.4, rho_in=1.0, p_in=1.0,
+                   rho_out=0.125, p_out=0.1):
+        U = g.zeros()
+        gc = g.c()
+        self.lib.orc_init_blast(_p(U), C.byref(gc), cx, cy, r, rho_in, p_in, rho_out, p_out)
+        return U
+
+    def init_shock_bubble(self, g: Grid, rho0=1.0, p0=1.0, mach=1.22, shock_x=0.005,
+                          bub_cx=0.035, bub_cy=0.0445, bub_r=0.025, rho_bubble=0.138):
+        U = g.zeros()
+        gc = g.c()
+        self.lib.orc_init_shock_bubble(_p(U), C.byref(gc), rho0, p0, mach, shock_x, bub_cx,
+                                       bub_cy, bub_r, rho_bubble)
+        return U
+
+    def init_reference_case(self, g: Grid, case_id: int):
+        U = g.zeros()
+        if self.kind == "port":
+            gc = g.c()
+            self.lib.orc_init_reference_case(_p(U), C.byref(gc), int(case_id))
+        else:
+            raise NotImplementedError("use ref_init_case via init_reference_n")
+        return U
+
+    def reference_case(self, case_id: int, n: int):
+        """(Grid, U0, cfl, t_end) of the reference's own case at scale n
+        (src/test_cases.cpp:132-195).  Reference build only."""
+        out = np.zeros(9)
+        self.lib.ref_case_config(int(case_id), int(n), _p(out))
+        g = Grid(int(out[0]), int(out[1]), out[3], out[4], out[5], out[6])
+        U = g.zeros()
+        self.lib.ref_init_case(int(case_id), int(n), _p(U))
+        return g, U, float(out[7]), float(out[8])

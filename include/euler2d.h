@@ -1,0 +1,160 @@
+/*
+ * euler2d.h -- C ABI of the GB300 (sm_103a) MUSCL-Hancock split step for the
+ * 2D compressible Euler equations.
+ *
+ * Drop-in boundary for the reference CPU/OpenMP solver.  The reference's C++
+ * surface is
+ *   double compute_dt(const Grid2D&, double cfl)                 src/cpu/solver_cpu.cpp:287-309
+ *   void advance_second_order(const Grid2D& Uold, Grid2D& Utmp,
+ *        Grid2D& Unew, double dt, CpuWorkspace&, RiemannSolver)  src/cpu/solver_cpu.cpp:400-499
+ *   void advance_first_order(...)                                src/cpu/solver_cpu.cpp:315-369
+ *   CaseConfig / get_n_case_config / initial_state_at            head/test_cases.hpp:8-35
+ * and its driver loop is scripts/cpu/main_cpu.cpp:206-262.  Each entry point
+ * below names the reference interface it replaces.  A C++ shim with the exact
+ * solver_cpu.hpp signatures sits on top of this ABI
+ * (large_sys_eq_opt_gb300/shim/solver_cpu_gb300.cpp).
+ *
+ * Conventions
+ *   - every function returns EU_OK (0) or an eu_status code; it never
+ *     throws and never exits.  eu_last_error(h) (h may be NULL for errors of
+ *     eu_create and the case helpers) gives a message.
+ *   - host grids ("AoS") use the reference Grid2D layout
+ *     (head/cpu/grid_cpu.hpp:10-89): 4 doubles per cell (rho, rhou, rhov, E),
+ *     (nx+4)*(ny+4) cells including the 2-cell ghost frame, cell (i, j) at
+ *     index j*(nx+4)+i.
+ *   - one handle = one grid, one CUDA stream, device-resident state.  A
+ *     handle is not thread-safe; several handles may be used concurrently.
+ *   - no CPU fallback: without a usable sm_103a device, eu_create fails.
+ */
+#ifndef EULER2D_H
+#define EULER2D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EU_ABI_VERSION 1
+
+typedef struct eu_handle eu_handle;
+
+typedef enum {
+    EU_OK = 0,
+    EU_ERR_INVALID = 1,     /* bad argument or configuration */
+    EU_ERR_CUDA = 2,        /* CUDA runtime/driver failure */
+    EU_ERR_NOMEM = 3,       /* device or pinned allocation failed */
+    EU_ERR_NONPHYSICAL = 4, /* maximum wave speed not positive / not finite
+                               (the reference throws std::runtime_error,
+                               src/cpu/solver_cpu.cpp:304-306) */
+    EU_ERR_TIMEOUT = 5,     /* a bounded device wait expired */
+    EU_ERR_STATE = 6        /* call not valid in the handle's current state */
+} eu_status;
+
+typedef enum { EU_FP64 = 0, EU_FP32 = 1 } eu_precision;
+
+/* Same order as RiemannSolver (head/riemann.hpp:13-18). */
+typedef enum { EU_HLL = 0, EU_HLLC = 1, EU_EXACT = 2, EU_FORCE = 3 } eu_solver;
+
+/* minmod is the reference's only limiter (src/cpu/solver_cpu.cpp:22-37). */
+typedef enum { EU_LIMITER_MINMOD = 0 } eu_limiter;
+
+/* Per-side boundary; the reference has transmissive only
+ * (head/cpu/boundary_cpu.hpp:5-37).  Reflective mirrors the two ghost layers
+ * and negates the normal momentum. */
+typedef enum { EU_BC_TRANSMISSIVE = 0, EU_BC_REFLECTIVE = 1 } eu_bc;
+enum { EU_SIDE_LEFT = 0, EU_SIDE_RIGHT = 1, EU_SIDE_BOTTOM = 2, EU_SIDE_TOP = 3 };
+
+/* CaseConfig (head/test_cases.hpp:8-18).  ng must be 2. */
+typedef struct {
+    int nx, ny, ng;
+    double x_min, x_max, y_min, y_max;
+    double cfl, t_end;
+} eu_case;
+
+typedef struct {
+    double t;           /* final simulation time */
+    long long steps;    /* steps taken */
+    int status;         /* device status bits (0 = clean) */
+    int nsnap_written;  /* snapshots delivered to the callback */
+} eu_run_info;
+
+/* Snapshot callback of eu_run: k = 1..nsnap, the step and time at which the
+ * reference writes it (first step with t >= t_end*k/nsnap,
+ * scripts/cpu/main_cpu.cpp:244-261) and the full grid in Grid2D AoS layout
+ * (valid during the call).  Return non-zero to abort the run. */
+typedef int (*eu_snapshot_cb)(void* user, int k, long long step, double t, const double* aos, int nx,
+                              int ny);
+
+/* ---- handle lifecycle ---------------------------------------------------- */
+/* Replaces Grid2D x3 + CpuWorkspace::init (scripts/cpu/main_cpu.cpp:175-191,
+ * head/cpu/solver_cpu.hpp:28-33).  bc: left, right, bottom, top (NULL = all
+ * transmissive). */
+int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limiter limiter, const int* bc,
+              eu_handle** out);
+void eu_destroy(eu_handle* h);
+const char* eu_last_error(const eu_handle* h);
+int eu_abi_version(void);
+
+/* ---- setup (src/test_cases.cpp, src/init.cpp) ---------------------------- */
+/* get_n_case_config (src/test_cases.cpp:184-195); name "shock_bubble" or
+ * "blast_wave"; unknown names fail like parse_case_id. */
+int eu_get_case_config(const char* name, int n, eu_case* out);
+/* initialise_grid with the reference case (src/init.cpp:29-38), on device. */
+int eu_init_reference_case(eu_handle* h, const char* name);
+/* Parameterised blast / shock-bubble states (src/test_cases.cpp:24-101), on device. */
+int eu_init_blast(eu_handle* h, double cx, double cy, double r, double rho_in, double p_in, double rho_out,
+                  double p_out);
+int eu_init_shock_bubble(eu_handle* h, double rho0, double p0, double mach, double shock_x, double bub_cx,
+                         double bub_cy, double bub_r, double rho_bubble);
+
+/* ---- state transfer -------------------------------------------------------- */
+int eu_upload_aos(eu_handle* h, const double* aos);   /* whole grid incl. ghosts */
+int eu_download_aos(eu_handle* h, double* aos);       /* ghosts filled by the BC rule */
+
+/* ---- the hot path ---------------------------------------------------------- */
+/* compute_dt (src/cpu/solver_cpu.cpp:287-309) on the device state. */
+int eu_compute_dt(eu_handle* h, double cfl, double* dt);
+/* advance_second_order (src/cpu/solver_cpu.cpp:400-499) on the device state:
+ * x-sweep, BC, y-sweep, BC, with the given dt. */
+int eu_advance(eu_handle* h, double dt);
+/* n steps device-resident in a CUDA graph.  dts == NULL: each dt from the
+ * fused CFL reduction (no t_end clip); otherwise the frozen list dts[0..n). */
+int eu_step_n(eu_handle* h, long long n, const double* dts);
+/* The time loop of scripts/cpu/main_cpu.cpp:206-262 from t = 0 on the current
+ * state: dt, t_end clip and snapshot schedule on the device, steps replayed
+ * from a CUDA graph, snapshots copied asynchronously and handed to cb. */
+int eu_run(eu_handle* h, double t_end, int nsnap, eu_snapshot_cb cb, void* user, eu_run_info* info);
+/* Current time, completed steps and the dt the next step would use. */
+int eu_get_time(eu_handle* h, double* t, long long* steps, double* dt_next);
+/* FP64 totals of rho, rhou, rhov, E over the interior (conserved audit). */
+int eu_totals(eu_handle* h, double out[4]);
+
+/* ---- drop-in calls on host grids (what the reference's callers pass) ------- */
+/* compute_dt(const Grid2D&, double): upload, reduce, read back dt. */
+int eu_compute_dt_host(eu_handle* h, const double* U, double cfl, double* dt);
+/* advance_second_order(Uold, Utmp, Unew, dt, ws, solver) on host grids:
+ * upload Uold, one step, download Unew (and Utmp when non-NULL). */
+int eu_advance_host(eu_handle* h, const double* Uold, double* Utmp, double* Unew, double dt);
+/* One iteration of the reference loop body on host grids
+ * (scripts/cpu/main_cpu.cpp:222-241): upload U, dt = compute_dt(U, cfl)
+ * clipped to t_end - t, advance, download into Unext; *dt_used returns dt. */
+int eu_step_host(eu_handle* h, const double* U, double* Unext, double cfl, double t, double t_end,
+                 double* dt_used);
+
+/* ---- measurement ------------------------------------------------------------- */
+/* Runs nsteps free-running CFL steps (one CUDA graph when use_graph) with
+ * CUDA events on the handle's stream around every kernel.  ms[0] = total
+ * elapsed, ms[1] = sum over x-sweep launches, ms[2] = sum over y-sweep
+ * launches. */
+int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]);
+/* Pinned host memory for zero-staging transfers. */
+int eu_host_alloc(size_t bytes, void** p);
+void eu_host_free(void* p);
+/* Name of device 0 and its SM count, for logs. */
+int eu_device_info(char* name, int len, int* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EULER2D_H */

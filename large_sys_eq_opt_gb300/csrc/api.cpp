@@ -1,0 +1,826 @@
+// api.cpp -- host runtime behind include/euler2d.h.
+//
+// One handle owns: two SoA state buffers (S0/S1, ping-pong), the x-sweep
+// output buffer Utmp, the device control block (Ctl), three TMA descriptors
+// (S0 and S1 boxed for the x-sweep, Utmp boxed for the y-sweep), a CUDA
+// stream, and lazily built CUDA graphs of whole steps.  The host never
+// touches a state value on the hot path: dt, t_end clipping and the snapshot
+// schedule live in Ctl and are advanced by the y-sweep's last warp.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/euler2d.h"
+#include "aux_kernels.h"
+
+using namespace eu;
+
+namespace {
+
+thread_local std::string g_err;
+
+long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+SweepKernels kernels_for(int prec, int solver) {
+    if (prec == EU_FP32) {
+        switch (solver) {
+            case EU_HLLC: return sweep_kernels_32_1();
+            case EU_EXACT: return sweep_kernels_32_2();
+            case EU_FORCE: return sweep_kernels_32_3();
+            default: return sweep_kernels_32_0();
+        }
+    }
+    switch (solver) {
+        case EU_HLLC: return sweep_kernels_64_1();
+        case EU_EXACT: return sweep_kernels_64_2();
+        case EU_FORCE: return sweep_kernels_64_3();
+        default: return sweep_kernels_64_0();
+    }
+}
+
+}  // namespace
+
+struct eu_handle {
+    eu_case cfg{};
+    int prec = EU_FP64, solver = EU_HLL;
+    int bc[4] = {0, 0, 0, 0};
+    size_t esz = 8;
+    double dx = 0, dy = 0;
+    int sm_count = 152;
+    cudaStream_t st = nullptr;
+    long long pitch_s = 0, plane_s = 0, pitch_t = 0, plane_t = 0;
+    void* S[2] = {nullptr, nullptr};
+    void* Tm = nullptr;
+    Ctl* ctl = nullptr;   // device
+    Ctl* hctl = nullptr;  // pinned host mirror
+    double* d_aos = nullptr;
+    double* h_aos = nullptr;  // pinned staging for snapshots
+    double* d_part = nullptr;
+    double* d_tot = nullptr;
+    double* h_tot = nullptr;
+    int part_blocks = 1024;
+    void* snap = nullptr;
+    long long snap_plane = 0, snap_stride = 0;
+    int snap_cap = 0;
+    double* d_frozen = nullptr;
+    long long frozen_cap = 0;
+    CUtensorMap tm_x[2];
+    CUtensorMap tm_y;
+    SweepKernels K{};
+    int seg_x = 0, nseg_x = 0, ntasks_x = 0, ctas_x = 0;
+    int seg_y = 0, nseg_y = 0, ntasks_y = 0, ctas_y = 0;
+    int cur = 0;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int gsteps = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(eu_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    else g_err = msg;
+    return code;
+}
+
+int cuda_fail(eu_handle* h, cudaError_t e, const char* what) {
+    return fail(h, e == cudaErrorMemoryAllocation ? EU_ERR_NOMEM : EU_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define EU_CUDA(h, call)                                        \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
+    } while (0)
+
+template <class T> Planes<T> planes_s(const eu_handle* h, int b) {
+    return Planes<T>{static_cast<T*>(h->S[b]), h->pitch_s, h->plane_s};
+}
+template <class T> Planes<T> planes_t(const eu_handle* h) {
+    return Planes<T>{static_cast<T*>(h->Tm), h->pitch_t, h->plane_t};
+}
+
+int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long pitch, long long plane,
+           int box_w, int box_h) {
+    auto fn = encode_fn();
+    if (!fn) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    const cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)(h->cfg.ny + 4), 4};
+    const cuuint64_t strides[2] = {(cuuint64_t)(pitch * h->esz), (cuuint64_t)(plane * h->esz)};
+    const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 4};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = fn(m, h->prec == EU_FP32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                          3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return EU_OK;
+}
+
+// Work decomposition: enough independent warps to fill every SM a few times
+// over, with segments long enough that the 4-cell halo per segment stays a
+// small fraction of the work.
+void plan(eu_handle* h) {
+    const int nx = h->cfg.nx, ny = h->cfg.ny;
+    const long long target = (long long)h->sm_count * 24;
+    const int W = 32 * h->K.vec_x;
+    const int max_seg = (nx + W - 1) / W;
+    int nseg = (int)std::min<long long>(std::max<long long>((target + ny - 1) / ny, 1), max_seg);
+    h->seg_x = (int)round_up((nx + nseg - 1) / nseg, W);
+    h->nseg_x = (nx + h->seg_x - 1) / h->seg_x;
+    h->ntasks_x = ny * h->nseg_x;
+    h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
+
+    const int WY = 32 * h->K.vec_y;
+    const int groups = (nx + h->K.off_y + WY - 1) / WY;
+    int nsy = (int)std::max<long long>((target + groups - 1) / groups, 1);
+    int segy = (ny + nsy - 1) / nsy;
+    segy = std::max(segy, std::min(ny, 64));
+    h->seg_y = segy;
+    h->nseg_y = groups;  // tasks per row segment
+    h->ntasks_y = groups * ((ny + segy - 1) / segy);
+    h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
+}
+
+template <class T> SweepArgs<T> x_args(const eu_handle* h, int cur) {
+    SweepArgs<T> a{};
+    a.out = planes_t<T>(h);
+    a.ctl = h->ctl;
+    a.nx = h->cfg.nx;
+    a.ny = h->cfg.ny;
+    a.seg = h->seg_x;
+    a.nseg = h->nseg_x;
+    a.ntasks = h->ntasks_x;
+    a.bc_lo = h->bc[EU_SIDE_BOTTOM];
+    a.bc_hi = h->bc[EU_SIDE_TOP];
+    a.out_index = cur;
+    a.finalize = 0;
+    a.d = h->dx;
+    a.snap = static_cast<T*>(h->snap);
+    a.snap_plane = h->snap_plane;
+    a.snap_stride = h->snap_stride;
+    return a;
+}
+
+template <class T> SweepArgs<T> y_args(const eu_handle* h, int cur) {
+    SweepArgs<T> a{};
+    a.out = planes_s<T>(h, 1 - cur);
+    a.ctl = h->ctl;
+    a.nx = h->cfg.nx;
+    a.ny = h->cfg.ny;
+    a.seg = h->seg_y;
+    a.nseg = h->nseg_y;
+    a.ntasks = h->ntasks_y;
+    a.bc_lo = h->bc[EU_SIDE_LEFT];
+    a.bc_hi = h->bc[EU_SIDE_RIGHT];
+    a.out_index = 1 - cur;
+    a.finalize = 1;
+    a.d = h->dy;
+    return a;
+}
+
+cudaError_t launch_x(eu_handle* h, int cur) {
+    if (h->prec == EU_FP32) {
+        const SweepArgs<float> a = x_args<float>(h, cur);
+        return h->K.x(&h->tm_x[cur], &a, h->ctas_x, h->st);
+    }
+    const SweepArgs<double> a = x_args<double>(h, cur);
+    return h->K.x(&h->tm_x[cur], &a, h->ctas_x, h->st);
+}
+
+cudaError_t launch_y(eu_handle* h, int cur) {
+    if (h->prec == EU_FP32) {
+        const SweepArgs<float> a = y_args<float>(h, cur);
+        return h->K.y(&h->tm_y, &a, h->ctas_y, h->st);
+    }
+    const SweepArgs<double> a = y_args<double>(h, cur);
+    return h->K.y(&h->tm_y, &a, h->ctas_y, h->st);
+}
+
+cudaError_t launch_step(eu_handle* h, int cur) {
+    cudaError_t e = launch_x(h, cur);
+    if (e != cudaSuccess) return e;
+    return launch_y(h, cur);
+}
+
+cudaError_t launch_dt(eu_handle* h, int b) {
+    if (h->prec == EU_FP32) return eu::launch_dt<float>(planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->ctl, h->st);
+    return eu::launch_dt<double>(planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->ctl, h->st);
+}
+
+cudaError_t unpack_state(eu_handle* h, int b, double* d_aos) {
+    if (h->prec == EU_FP32)
+        return launch_unpack_aos<float>(planes_s<float>(h, b), 2, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+    return launch_unpack_aos<double>(planes_s<double>(h, b), 2, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+}
+
+cudaError_t unpack_tmp(eu_handle* h, double* d_aos) {
+    if (h->prec == EU_FP32)
+        return launch_unpack_aos<float>(planes_t<float>(h), 4, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+    return launch_unpack_aos<double>(planes_t<double>(h), 4, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+}
+
+cudaError_t pack_state(eu_handle* h, int b, const double* d_aos) {
+    if (h->prec == EU_FP32) return launch_pack_aos<float>(d_aos, planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->st);
+    return launch_pack_aos<double>(d_aos, planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->st);
+}
+
+long long aos_bytes(const eu_handle* h) { return 32LL * (h->cfg.nx + 4) * (h->cfg.ny + 4); }
+
+// Control block defaults for a fresh sequence of steps.
+void ctl_reset(eu_handle* h, int mode, double t_end, long long max_steps) {
+    Ctl& c = *h->hctl;
+    std::memset(&c, 0, sizeof(Ctl));
+    c.t = 0.0;
+    c.dt = 0.0;
+    c.t_end = t_end;
+    c.cfl_dmin = h->cfg.cfl * std::min(h->dx, h->dy);
+    c.mode = mode;
+    c.max_steps = max_steps;
+    c.cur = h->cur;
+}
+
+int ctl_push(eu_handle* h) {
+    EU_CUDA(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->st));
+    return EU_OK;
+}
+
+int ctl_pull_sync(eu_handle* h) {
+    EU_CUDA(h, cudaMemcpyAsync(h->hctl, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    h->cur = h->hctl->cur;
+    return EU_OK;
+}
+
+int status_code(eu_handle* h) {
+    const int s = h->hctl->status;
+    if (s & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
+    if (s & kStatusNonPhysical) return fail(h, EU_ERR_NONPHYSICAL, "compute_dt: non-positive maximum wave speed.");
+    return EU_OK;
+}
+
+// Graph of `steps` consecutive steps starting from buffer `cur`.
+int build_graph(eu_handle* h, int cur, int steps, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    EU_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < steps && e == cudaSuccess; ++s) e = launch_step(h, (cur + s) & 1);
+    cudaError_t e2 = cudaStreamEndCapture(h->st, &g);
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(h, e, "step capture"); }
+    if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    return EU_OK;
+}
+
+int graph_for(eu_handle* h, int cur, cudaGraphExec_t* out) {
+    if (!h->gexec[cur]) {
+        int rc = build_graph(h, cur, h->gsteps, &h->gexec[cur]);
+        if (rc) return rc;
+    }
+    *out = h->gexec[cur];
+    return EU_OK;
+}
+
+void drop_graphs(eu_handle* h) {
+    for (auto& g : h->gexec)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+int ensure_aos(eu_handle* h) {
+    if (!h->d_aos) EU_CUDA(h, cudaMalloc(&h->d_aos, aos_bytes(h)));
+    return EU_OK;
+}
+
+int ensure_snapshots(eu_handle* h, int nsnap) {
+    if (nsnap <= h->snap_cap) return EU_OK;
+    if (h->snap) { cudaFree(h->snap); h->snap = nullptr; h->snap_cap = 0; }
+    h->snap_plane = (long long)h->cfg.nx * h->cfg.ny;
+    h->snap_stride = 4 * h->snap_plane;
+    EU_CUDA(h, cudaMalloc(&h->snap, (size_t)nsnap * h->snap_stride * h->esz));
+    h->snap_cap = nsnap;
+    drop_graphs(h);  // graphs bake the snapshot pointer into the x-sweep args
+    if (!h->h_aos) EU_CUDA(h, cudaMallocHost(&h->h_aos, aos_bytes(h)));
+    return ensure_aos(h);
+}
+
+int upload_to(eu_handle* h, int b, const double* aos) {
+    int rc = ensure_aos(h);
+    if (rc) return rc;
+    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, aos, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
+    EU_CUDA(h, pack_state(h, b, h->d_aos));
+    return EU_OK;
+}
+
+int download_from_state(eu_handle* h, int b, double* aos) {
+    int rc = ensure_aos(h);
+    if (rc) return rc;
+    EU_CUDA(h, unpack_state(h, b, h->d_aos));
+    EU_CUDA(h, cudaMemcpyAsync(aos, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
+    return EU_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int eu_abi_version(void) { return EU_ABI_VERSION; }
+
+const char* eu_last_error(const eu_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int eu_device_info(char* name, int len, int* sm_count) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(nullptr, EU_ERR_CUDA, "no CUDA device");
+    cudaDeviceProp p;
+    EU_CUDA(nullptr, cudaGetDeviceProperties(&p, 0));
+    if (name && len > 0) std::snprintf(name, (size_t)len, "%s (sm_%d%d)", p.name, p.major, p.minor);
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    return EU_OK;
+}
+
+int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limiter limiter, const int* bc,
+              eu_handle** out) {
+    if (!cfg || !out) return fail(nullptr, EU_ERR_INVALID, "eu_create: null argument");
+    *out = nullptr;
+    if (cfg->nx < 1 || cfg->ny < 1) return fail(nullptr, EU_ERR_INVALID, "eu_create: nx and ny must be >= 1");
+    if (cfg->ng != 2) return fail(nullptr, EU_ERR_INVALID, "eu_create: ghost width ng must be 2");
+    if (!(cfg->x_max > cfg->x_min) || !(cfg->y_max > cfg->y_min))
+        return fail(nullptr, EU_ERR_INVALID, "eu_create: empty domain");
+    if (prec != EU_FP64 && prec != EU_FP32) return fail(nullptr, EU_ERR_INVALID, "eu_create: bad precision");
+    if (solver < EU_HLL || solver > EU_FORCE) return fail(nullptr, EU_ERR_INVALID, "eu_create: bad solver");
+    if (limiter != EU_LIMITER_MINMOD) return fail(nullptr, EU_ERR_INVALID, "eu_create: only minmod is provided");
+    if ((long long)cfg->nx * cfg->ny > (1LL << 31) - 1 || cfg->nx > (1 << 28) || cfg->ny > (1 << 28))
+        return fail(nullptr, EU_ERR_INVALID, "eu_create: grid too large");
+    int b4[4] = {0, 0, 0, 0};
+    if (bc)
+        for (int k = 0; k < 4; ++k) {
+            if (bc[k] != EU_BC_TRANSMISSIVE && bc[k] != EU_BC_REFLECTIVE)
+                return fail(nullptr, EU_ERR_INVALID, "eu_create: bad boundary kind");
+            b4[k] = bc[k];
+        }
+    if ((b4[0] || b4[1]) && cfg->nx < 2) return fail(nullptr, EU_ERR_INVALID, "reflective x sides need nx >= 2");
+    if ((b4[2] || b4[3]) && cfg->ny < 2) return fail(nullptr, EU_ERR_INVALID, "reflective y sides need ny >= 2");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, EU_ERR_CUDA, "eu_create: no CUDA device (this library has no CPU path)");
+    int dev = 0, major = 0, minor = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3)
+        return fail(nullptr, EU_ERR_CUDA,
+                    "eu_create: kernels are built for sm_103a; device is sm_" + std::to_string(major) +
+                        std::to_string(minor));
+
+    eu_handle* h = new eu_handle();
+    h->cfg = *cfg;
+    h->prec = prec;
+    h->solver = solver;
+    std::memcpy(h->bc, b4, sizeof(b4));
+    h->esz = prec == EU_FP32 ? 4 : 8;
+    h->dx = (cfg->x_max - cfg->x_min) / (double)cfg->nx;  // head/cpu/grid_cpu.hpp:19-20
+    h->dy = (cfg->y_max - cfg->y_min) / (double)cfg->ny;
+    cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    h->K = kernels_for(prec, solver);
+    h->gsteps = 2;
+    plan(h);
+
+    auto bail = [&](int rc) {
+        eu_destroy(h);
+        return rc;
+    };
+    const long long align = 128 / (long long)h->esz;
+    h->pitch_s = round_up(cfg->nx + 4, align);
+    h->pitch_t = round_up(cfg->nx + 8, align);
+    h->plane_s = round_up(h->pitch_s * (cfg->ny + 4), 256 / (long long)h->esz);
+    h->plane_t = round_up(h->pitch_t * (cfg->ny + 4), 256 / (long long)h->esz);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return bail(EU_ERR_CUDA); }
+    for (int b = 0; b < 2; ++b) {
+        e = cudaMalloc(&h->S[b], (size_t)(4 * h->plane_s) * h->esz);
+        if (e == cudaSuccess) e = cudaMemsetAsync(h->S[b], 0, (size_t)(4 * h->plane_s) * h->esz, h->st);
+        if (e != cudaSuccess) { g_err = std::string("state buffer: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
+    }
+    e = cudaMalloc(&h->Tm, (size_t)(4 * h->plane_t) * h->esz);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->Tm, 0, (size_t)(4 * h->plane_t) * h->esz, h->st);
+    if (e == cudaSuccess) e = cudaMalloc(&h->ctl, sizeof(Ctl));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->hctl, sizeof(Ctl));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_part, sizeof(double) * 8 * h->part_blocks);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_tot, sizeof(double) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_tot, sizeof(double) * 4);
+    if (e != cudaSuccess) { g_err = std::string("allocation: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
+    ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
+    if (ctl_push(h)) { g_err = h->err; return bail(EU_ERR_CUDA); }
+    for (int b = 0; b < 2; ++b)
+        if (encode(h, &h->tm_x[b], h->S[b], cfg->nx + 4, h->pitch_s, h->plane_s, 32 * h->K.vec_x, 1)) {
+            g_err = h->err;
+            return bail(EU_ERR_CUDA);
+        }
+    if (encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry)) {
+        g_err = h->err;
+        return bail(EU_ERR_CUDA);
+    }
+    e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) { g_err = std::string("eu_create: ") + cudaGetErrorString(e); return bail(EU_ERR_CUDA); }
+    *out = h;
+    return EU_OK;
+}
+
+void eu_destroy(eu_handle* h) {
+    if (!h) return;
+    if (h->st) cudaStreamSynchronize(h->st);
+    drop_graphs(h);
+    cudaFree(h->S[0]);
+    cudaFree(h->S[1]);
+    cudaFree(h->Tm);
+    cudaFree(h->ctl);
+    cudaFreeHost(h->hctl);
+    cudaFree(h->d_aos);
+    cudaFreeHost(h->h_aos);
+    cudaFree(h->d_part);
+    cudaFree(h->d_tot);
+    cudaFreeHost(h->h_tot);
+    cudaFree(h->snap);
+    cudaFree(h->d_frozen);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+// --- setup ------------------------------------------------------------------
+int eu_get_case_config(const char* name, int n, eu_case* out) {
+    if (!name || !out) return fail(nullptr, EU_ERR_INVALID, "eu_get_case_config: null argument");
+    if (n < 1) return fail(nullptr, EU_ERR_INVALID, "get_n_case_config: n must be >= 1.");
+    const std::string s(name);
+    // src/test_cases.cpp:132-162
+    if (s == "shock_bubble") *out = eu_case{500, 197, 2, 0.0, 0.225, 0.0, 0.089, 0.4, 0.0011741};
+    else if (s == "blast_wave") *out = eu_case{500, 500, 2, 0.0, 1.0, 0.0, 1.0, 0.4, 0.2};
+    else
+        return fail(nullptr, EU_ERR_INVALID,
+                    "Unknown case name: " + s + ". Supported cases are: shock_bubble, blast_wave.");
+    out->nx *= n;  // src/test_cases.cpp:184-195
+    out->ny *= n;
+    return EU_OK;
+}
+
+int eu_init_blast(eu_handle* h, double cx, double cy, double r, double rho_in, double p_in, double rho_out,
+                  double p_out) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    const GridGeom g{h->cfg.nx, h->cfg.ny, h->cfg.x_min, h->cfg.x_max, h->cfg.y_min, h->cfg.y_max};
+    const BlastDesc b{cx, cy, r, rho_in, p_in, rho_out, p_out};
+    if (h->prec == EU_FP32) EU_CUDA(h, launch_init_blast<float>(planes_s<float>(h, h->cur), g, b, h->st));
+    else EU_CUDA(h, launch_init_blast<double>(planes_s<double>(h, h->cur), g, b, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_init_shock_bubble(eu_handle* h, double rho0, double p0, double mach, double shock_x, double bub_cx,
+                         double bub_cy, double bub_r, double rho_bubble) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    const GridGeom g{h->cfg.nx, h->cfg.ny, h->cfg.x_min, h->cfg.x_max, h->cfg.y_min, h->cfg.y_max};
+    const ShockBubbleDesc d{rho0, p0, mach, shock_x, bub_cx, bub_cy, bub_r, rho_bubble};
+    if (h->prec == EU_FP32) EU_CUDA(h, launch_init_shock_bubble<float>(planes_s<float>(h, h->cur), g, d, h->st));
+    else EU_CUDA(h, launch_init_shock_bubble<double>(planes_s<double>(h, h->cur), g, d, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_init_reference_case(eu_handle* h, const char* name) {
+    if (!h || !name) return fail(h, EU_ERR_INVALID, "null argument");
+    const std::string s(name);
+    // src/test_cases.cpp:24-33 and :79-89
+    if (s == "shock_bubble") return eu_init_shock_bubble(h, 1.29, 1.01325e5, 1.22, 0.005, 0.035, 0.0445, 0.025, 0.214);
+    if (s == "blast_wave") return eu_init_blast(h, 0.5, 0.5, 0.1, 1.0, 100.0, 1.0, 1.0);
+    return fail(h, EU_ERR_INVALID, "Unknown case name: " + s + ". Supported cases are: shock_bubble, blast_wave.");
+}
+
+// --- transfer -------------------------------------------------------------
+int eu_upload_aos(eu_handle* h, const double* aos) {
+    if (!h || !aos) return fail(h, EU_ERR_INVALID, "null argument");
+    int rc = upload_to(h, h->cur, aos);
+    if (rc) return rc;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_download_aos(eu_handle* h, double* aos) {
+    if (!h || !aos) return fail(h, EU_ERR_INVALID, "null argument");
+    int rc = download_from_state(h, h->cur, aos);
+    if (rc) return rc;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+// --- hot path -----------------------------------------------------------------
+int eu_compute_dt(eu_handle* h, double cfl, double* dt) {
+    if (!h || !dt) return fail(h, EU_ERR_INVALID, "null argument");
+    if (!(cfl > 0.0)) return fail(h, EU_ERR_INVALID, "cfl must be positive");
+    Ctl& c = *h->hctl;
+    c.mode = kModeHost;
+    c.cfl_dmin = cfl * std::min(h->dx, h->dy);
+    c.done = 0;
+    c.status = 0;
+    c.smax_bits = 0;
+    c.arrive = 0;
+    c.max_steps = LLONG_MAX;
+    int rc = ctl_push(h);
+    if (rc) return rc;
+    EU_CUDA(h, launch_dt(h, h->cur));
+    rc = ctl_pull_sync(h);
+    if (rc) return rc;
+    rc = status_code(h);
+    if (rc) return rc;
+    *dt = c.dt;
+    return EU_OK;
+}
+
+int eu_advance(eu_handle* h, double dt) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (!(dt >= 0.0) || !std::isfinite(dt)) return fail(h, EU_ERR_INVALID, "dt must be finite and >= 0");
+    Ctl& c = *h->hctl;
+    c.mode = kModeHost;
+    c.dt = dt;
+    c.done = 0;
+    c.status = 0;
+    c.smax_bits = 0;
+    c.arrive = 0;
+    c.max_steps = LLONG_MAX;
+    c.snap_req = 0;
+    c.nsnap = 0;
+    c.cur = h->cur;
+    int rc = ctl_push(h);
+    if (rc) return rc;
+    EU_CUDA(h, launch_step(h, h->cur));
+    rc = ctl_pull_sync(h);
+    if (rc) return rc;
+    return h->hctl->status & kStatusTimeout ? status_code(h) : EU_OK;
+}
+
+int eu_step_n(eu_handle* h, long long n, const double* dts) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (n < 0) return fail(h, EU_ERR_INVALID, "n must be >= 0");
+    if (n == 0) return EU_OK;
+    Ctl& c = *h->hctl;
+    const double t0 = c.t;
+    const long long s0 = c.step;
+    ctl_reset(h, dts ? kModeFrozen : kModeCfl, INFINITY, s0 + n);
+    c.t = t0;
+    c.step = s0;
+    if (dts) {
+        if (n > h->frozen_cap) {
+            cudaFree(h->d_frozen);
+            h->d_frozen = nullptr;
+            h->frozen_cap = 0;
+            EU_CUDA(h, cudaMalloc(&h->d_frozen, sizeof(double) * (size_t)n));
+            h->frozen_cap = n;
+        }
+        EU_CUDA(h, cudaMemcpyAsync(h->d_frozen, dts, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->st));
+        c.frozen = h->d_frozen;
+        c.n_frozen = n;
+        c.frozen_base = s0;
+        c.dt = dts[0];
+    }
+    int rc = ctl_push(h);
+    if (rc) return rc;
+    if (!dts) EU_CUDA(h, launch_dt(h, h->cur));
+    const int K = h->gsteps;
+    const long long reps = (n + K - 1) / K;
+    cudaGraphExec_t g = nullptr;
+    int cur = h->cur;
+    for (long long r = 0; r < reps; ++r) {
+        // Replays of a K-step graph; steps past the end are no-ops (Ctl::done).
+        rc = graph_for(h, cur, &g);
+        if (rc) return rc;
+        EU_CUDA(h, cudaGraphLaunch(g, h->st));
+        cur = (cur + K) & 1;
+    }
+    rc = ctl_pull_sync(h);
+    if (rc) return rc;
+    return status_code(h);
+}
+
+int eu_run(eu_handle* h, double t_end, int nsnap, eu_snapshot_cb cb, void* user, eu_run_info* info) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (nsnap < 0 || nsnap > kMaxSnap) return fail(h, EU_ERR_INVALID, "nsnap must be in [0, 16]");
+    if (!(t_end >= 0.0)) return fail(h, EU_ERR_INVALID, "t_end must be >= 0");
+    const bool want = cb && nsnap > 0;
+    int rc = EU_OK;
+    if (want && (rc = ensure_snapshots(h, nsnap))) return rc;
+    ctl_reset(h, kModeCfl, t_end, LLONG_MAX);
+    Ctl& c = *h->hctl;
+    c.nsnap = want ? nsnap : 0;  // without storage no snapshot is ever requested
+    for (int k = 0; k < nsnap; ++k) c.snap_target[k] = t_end * (double)(k + 1) / (double)nsnap;  // main_cpu.cpp:210-215
+    if ((rc = ctl_push(h))) return rc;
+    EU_CUDA(h, launch_dt(h, h->cur));
+    if ((rc = ctl_pull_sync(h))) return rc;
+    int delivered = 0;
+    bool aborted = false;
+    while (!c.done) {
+        cudaGraphExec_t g = nullptr;
+        if ((rc = graph_for(h, h->cur, &g))) return rc;
+        EU_CUDA(h, cudaGraphLaunch(g, h->st));
+        if ((rc = ctl_pull_sync(h))) return rc;
+        // hand over every snapshot whose copy is complete
+        while (want && !aborted && delivered < c.next_snap) {
+            const int k = delivered;
+            const long long sstep = c.snap_step[k];
+            if (!(c.step > sstep || c.done)) break;
+            int kb = k;
+            while (kb > 0 && c.snap_step[kb - 1] == sstep) --kb;
+            if (c.step > sstep) {
+                const long long plane = h->snap_plane;
+                if (h->prec == EU_FP32)
+                    EU_CUDA(h, launch_unpack_snapshot<float>(static_cast<float*>(h->snap) + kb * h->snap_stride, plane,
+                                                             h->cfg.nx, h->cfg.ny, h->bc, h->d_aos, h->st));
+                else
+                    EU_CUDA(h, launch_unpack_snapshot<double>(static_cast<double*>(h->snap) + kb * h->snap_stride,
+                                                              plane, h->cfg.nx, h->cfg.ny, h->bc, h->d_aos, h->st));
+            } else {
+                EU_CUDA(h, unpack_state(h, h->cur, h->d_aos));
+            }
+            EU_CUDA(h, cudaMemcpyAsync(h->h_aos, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
+            EU_CUDA(h, cudaStreamSynchronize(h->st));
+            if (cb(user, k + 1, sstep, c.snap_time[k], h->h_aos, h->cfg.nx, h->cfg.ny)) aborted = true;
+            ++delivered;
+        }
+        if (aborted || c.status) break;
+    }
+    if (info) {
+        info->t = c.t;
+        info->steps = c.step;
+        info->status = c.status;
+        info->nsnap_written = delivered;
+    }
+    if (aborted) return fail(h, EU_ERR_STATE, "run aborted by the snapshot callback");
+    return status_code(h);
+}
+
+int eu_get_time(eu_handle* h, double* t, long long* steps, double* dt_next) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    int rc = ctl_pull_sync(h);
+    if (rc) return rc;
+    if (t) *t = h->hctl->t;
+    if (steps) *steps = h->hctl->step;
+    if (dt_next) *dt_next = h->hctl->dt;
+    return EU_OK;
+}
+
+int eu_totals(eu_handle* h, double out[4]) {
+    if (!h || !out) return fail(h, EU_ERR_INVALID, "null argument");
+    if (h->prec == EU_FP32)
+        EU_CUDA(h, launch_totals<float>(planes_s<float>(h, h->cur), 2, h->cfg.nx, h->cfg.ny, h->d_part, h->part_blocks,
+                                        h->d_tot, h->st));
+    else
+        EU_CUDA(h, launch_totals<double>(planes_s<double>(h, h->cur), 2, h->cfg.nx, h->cfg.ny, h->d_part,
+                                         h->part_blocks, h->d_tot, h->st));
+    EU_CUDA(h, cudaMemcpyAsync(h->h_tot, h->d_tot, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    std::memcpy(out, h->h_tot, 4 * sizeof(double));
+    return EU_OK;
+}
+
+// --- drop-in calls on host grids -----------------------------------------------
+int eu_compute_dt_host(eu_handle* h, const double* U, double cfl, double* dt) {
+    if (!h || !U || !dt) return fail(h, EU_ERR_INVALID, "null argument");
+    int rc = upload_to(h, h->cur, U);
+    if (rc) return rc;
+    return eu_compute_dt(h, cfl, dt);
+}
+
+int eu_advance_host(eu_handle* h, const double* Uold, double* Utmp, double* Unew, double dt) {
+    if (!h || !Uold || !Unew) return fail(h, EU_ERR_INVALID, "null argument");
+    int rc = upload_to(h, h->cur, Uold);
+    if (rc) return rc;
+    if ((rc = eu_advance(h, dt))) return rc;
+    if (Utmp) {
+        EU_CUDA(h, unpack_tmp(h, h->d_aos));
+        EU_CUDA(h, cudaMemcpyAsync(Utmp, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
+    }
+    if ((rc = download_from_state(h, h->cur, Unew))) return rc;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_step_host(eu_handle* h, const double* U, double* Unext, double cfl, double t, double t_end,
+                 double* dt_used) {
+    if (!h || !U || !Unext) return fail(h, EU_ERR_INVALID, "null argument");
+    int rc = upload_to(h, h->cur, U);
+    if (rc) return rc;
+    ctl_reset(h, kModeCfl, t_end, LLONG_MAX);
+    Ctl& c = *h->hctl;
+    c.cfl_dmin = cfl * std::min(h->dx, h->dy);
+    c.t = t;
+    if ((rc = ctl_push(h))) return rc;
+    EU_CUDA(h, launch_dt(h, h->cur));           // dt = compute_dt(U), clipped to t_end - t
+    EU_CUDA(h, cudaMemcpyAsync(&h->hctl->dt, &h->ctl->dt, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    EU_CUDA(h, launch_step(h, h->cur));
+    const int nxt = 1 - h->cur;
+    if ((rc = download_from_state(h, nxt, Unext))) return rc;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    if (dt_used) *dt_used = h->hctl->dt;
+    rc = ctl_pull_sync(h);
+    if (rc) return rc;
+    return status_code(h);
+}
+
+// --- measurement ----------------------------------------------------------------
+int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
+    if (!h || !ms || nsteps < 1) return fail(h, EU_ERR_INVALID, "bad argument");
+    Ctl& c = *h->hctl;
+    const double t0 = c.t;
+    const long long s0 = c.step;
+    ctl_reset(h, kModeCfl, INFINITY, LLONG_MAX);
+    c.t = t0;
+    c.step = s0;
+    int rc = ctl_push(h);
+    if (rc) return rc;
+    EU_CUDA(h, launch_dt(h, h->cur));
+    std::vector<cudaEvent_t> ev(2 * (size_t)nsteps + 1, nullptr);
+    for (auto& e : ev) EU_CUDA(h, cudaEventCreate(&e));
+    auto cleanup = [&]() { for (auto& e : ev) if (e) cudaEventDestroy(e); };
+    cudaError_t e = cudaSuccess;
+    int cur = h->cur;
+    if (use_graph) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t gx = nullptr;
+        e = cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal);
+        for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
+            const int cc = (cur + s) & 1;
+            if (s == 0) e = cudaEventRecordWithFlags(ev[0], h->st, cudaEventRecordExternal);
+            if (e == cudaSuccess) e = launch_x(h, cc);
+            if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[2 * s + 1], h->st, cudaEventRecordExternal);
+            if (e == cudaSuccess) e = launch_y(h, cc);
+            if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[2 * s + 2], h->st, cudaEventRecordExternal);
+        }
+        cudaError_t e2 = cudaStreamEndCapture(h->st, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gx, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e == cudaSuccess) e = cudaGraphLaunch(gx, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        if (gx) cudaGraphExecDestroy(gx);
+    } else {
+        e = cudaEventRecord(ev[0], h->st);
+        for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
+            const int cc = (cur + s) & 1;
+            e = launch_x(h, cc);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[2 * s + 1], h->st);
+            if (e == cudaSuccess) e = launch_y(h, cc);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[2 * s + 2], h->st);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    }
+    if (e != cudaSuccess) { cleanup(); return cuda_fail(h, e, "eu_time_steps"); }
+    float tot = 0, tx = 0, ty = 0, v = 0;
+    cudaEventElapsedTime(&tot, ev[0], ev[2 * nsteps]);
+    for (int s = 0; s < nsteps; ++s) {
+        cudaEventElapsedTime(&v, ev[2 * s], ev[2 * s + 1]);
+        tx += v;
+        cudaEventElapsedTime(&v, ev[2 * s + 1], ev[2 * s + 2]);
+        ty += v;
+    }
+    cleanup();
+    ms[0] = tot;
+    ms[1] = tx;
+    ms[2] = ty;
+    rc = ctl_pull_sync(h);
+    if (rc) return rc;
+    return status_code(h);
+}
+
+int eu_host_alloc(size_t bytes, void** p) {
+    if (!p) return fail(nullptr, EU_ERR_INVALID, "null argument");
+    cudaError_t e = cudaMallocHost(p, bytes);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMallocHost");
+    return EU_OK;
+}
+
+void eu_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

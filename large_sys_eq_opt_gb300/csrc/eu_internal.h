@@ -1,0 +1,87 @@
+// eu_internal.h -- device control block and launch descriptors shared by the
+// sweep kernels and the host runtime (not part of the public C ABI).
+#pragma once
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace eu {
+
+constexpr int kMaxSnap = 16;
+
+// Device-resident step control.  One per handle, in device memory.  The
+// y-sweep's last warp (last-block-done, no spin) turns the step's maximum
+// signal speed into the next dt, advances t, applies the t_end clip and the
+// snapshot schedule of scripts/cpu/main_cpu.cpp:206-262, so dt never goes
+// back to the host.
+struct Ctl {
+    double t;            // simulation time at the start of the next step
+    double dt;           // step size the next step will use
+    double t_end;        // +inf for free-running steps
+    double cfl_dmin;     // cfl * min(dx, dy)
+    double smax;         // last reduced maximum signal speed (diagnostic)
+    const double* frozen;  // frozen dt list (mode kModeFrozen)
+    long long n_frozen;
+    long long frozen_base;  // step index of frozen[0]
+    long long max_steps; // done once step reaches this
+    long long step;      // completed steps
+    unsigned long long smax_bits;  // running max (bit pattern of a non-negative double)
+    unsigned int arrive;           // warps finished in the current launch
+    int done;            // 1 once t >= t_end, the frozen list is exhausted or on error
+    int status;          // kStatus* bits
+    int mode;            // kModeCfl / kModeFrozen / kModeHost
+    int cur;             // state buffer (0/1) holding the latest state
+    int nsnap, next_snap;
+    unsigned int snap_req;   // bit k: snapshot k is the state at the start of the next step
+    unsigned int snap_taken; // bit k: copied into snapshot storage
+    int pad;
+    double snap_target[kMaxSnap];
+    double snap_time[kMaxSnap];
+    long long snap_step[kMaxSnap];
+};
+
+enum { kModeCfl = 0, kModeFrozen = 1, kModeHost = 2 };
+enum { kStatusOk = 0, kStatusNonPhysical = 1, kStatusTimeout = 2, kStatusNonFinite = 4 };
+
+// SoA plane set: field f (0 rho, 1 rhou, 2 rhov, 3 E), array row r, column c
+// at base[f*plane + r*pitch + c].
+template <class T> struct Planes {
+    T* base;
+    long long pitch;
+    long long plane;
+};
+
+// Boundary kinds, as in include/euler2d.h.
+enum { kBcTransmissive = 0, kBcReflective = 1 };
+
+template <class T> struct SweepArgs {
+    Planes<T> out;       // x-sweep: Utmp (interior at col+4,row+2); y-sweep: Unew (col+2,row+2)
+    Ctl* ctl;
+    int nx, ny;
+    int seg;             // outputs per task along the march direction
+    int nseg;            // tasks per line
+    int ntasks;
+    int bc_lo, bc_hi;    // x-sweep: bottom/top; y-sweep: left/right (ghost lines it writes)
+    int out_index;       // y-sweep: index of the buffer it writes (becomes Ctl::cur)
+    int finalize;        // y-sweep: 1 = advance t/step and compute the next dt
+    double d;            // dx (x-sweep) or dy (y-sweep); the step uses dt/d
+    T* snap;             // x-sweep: snapshot storage, interior SoA [k][f][ny][nx]
+    long long snap_plane, snap_stride;
+};
+
+// Host-side launch entry of one sweep instantiation.
+using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const void* args, int ctas,
+                                    cudaStream_t s);
+
+struct SweepKernels {
+    SweepLaunch x, y;
+    int vec_x, vec_y;    // cells per lane
+    int off_y;           // interior column of lane 0 in y-sweep group 0 is -off_y
+    int ry;              // rows per y-sweep TMA box
+    int box_w_y;         // y-sweep box width in elements
+    int stages_x, stages_y;
+    int nw;              // warps per CTA
+    size_t smem_x, smem_y;
+};
+
+}  // namespace eu

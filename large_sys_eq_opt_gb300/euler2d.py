@@ -1,0 +1,291 @@
+"""Python binding of the C ABI (include/euler2d.h) -- a thin ctypes layer.
+
+The product is libeuler2d.so (hand-written sm_103a kernels + C++ runtime);
+this module only marshals arguments.  There is no CPU fallback: loading fails
+loudly when the library is missing, and creating a solver fails when no
+sm_103a GPU is present.
+
+The surface mirrors the reference's solver API:
+    Solver.compute_dt(cfl)                 compute_dt        (src/cpu/solver_cpu.cpp:287-309)
+    Solver.advance(dt)                     advance_second_order (src/cpu/solver_cpu.cpp:400-499)
+    Solver.advance_host(Uold, dt)          the same on host Grid2D arrays
+    Solver.run(t_end, nsnap, callback)     the time loop of scripts/cpu/main_cpu.cpp:206-262
+Host grids are float64 numpy arrays of shape (ny+4, nx+4, 4) -- the Grid2D
+AoS layout of head/cpu/grid_cpu.hpp:10-89.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .cases import BlastParams, CaseConfig, Problem, ShockBubbleParams
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libeuler2d.so")
+
+FP64, FP32 = 0, 1
+SOLVERS = {"hll": 0, "hllc": 1, "exact": 2, "force": 3}
+ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "non-physical state",
+          5: "device wait timed out", 6: "bad state"}
+
+_dp = C.POINTER(C.c_double)
+
+
+class EuCase(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("ng", C.c_int),
+                ("x_min", C.c_double), ("x_max", C.c_double), ("y_min", C.c_double), ("y_max", C.c_double),
+                ("cfl", C.c_double), ("t_end", C.c_double)]
+
+
+class EuRunInfo(C.Structure):
+    _fields_ = [("t", C.c_double), ("steps", C.c_longlong), ("status", C.c_int), ("nsnap_written", C.c_int)]
+
+
+SNAP_CB = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_longlong, C.c_double, _dp, C.c_int, C.c_int)
+
+# Every symbol include/euler2d.h declares (checked by the CPU test suite).
+EXPORTS = (
+    "eu_create", "eu_destroy", "eu_last_error", "eu_abi_version", "eu_get_case_config",
+    "eu_init_reference_case", "eu_init_blast", "eu_init_shock_bubble", "eu_upload_aos",
+    "eu_download_aos", "eu_compute_dt", "eu_advance", "eu_step_n", "eu_run", "eu_get_time",
+    "eu_totals", "eu_compute_dt_host", "eu_advance_host", "eu_step_host", "eu_time_steps",
+    "eu_host_alloc", "eu_host_free", "eu_device_info",
+)
+
+_lib = None
+
+
+class EulerError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{ERRORS.get(code, code)}] {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH):
+    """Load libeuler2d.so (build it first with large_sys_eq_opt_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: the CUDA library must be built (python -c 'import __graft_entry__ as g; "
+            "g.build()'); there is no CPU fallback")
+    L = C.CDLL(path)
+    H = C.c_void_p
+    L.eu_create.argtypes = [C.POINTER(EuCase), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(H)]
+    L.eu_destroy.argtypes = [H]
+    L.eu_destroy.restype = None
+    L.eu_last_error.argtypes = [H]
+    L.eu_last_error.restype = C.c_char_p
+    L.eu_abi_version.restype = C.c_int
+    L.eu_get_case_config.argtypes = [C.c_char_p, C.c_int, C.POINTER(EuCase)]
+    L.eu_init_reference_case.argtypes = [H, C.c_char_p]
+    L.eu_init_blast.argtypes = [H] + [C.c_double] * 7
+    L.eu_init_shock_bubble.argtypes = [H] + [C.c_double] * 8
+    L.eu_upload_aos.argtypes = [H, _dp]
+    L.eu_download_aos.argtypes = [H, _dp]
+    L.eu_compute_dt.argtypes = [H, C.c_double, _dp]
+    L.eu_advance.argtypes = [H, C.c_double]
+    L.eu_step_n.argtypes = [H, C.c_longlong, _dp]
+    L.eu_run.argtypes = [H, C.c_double, C.c_int, SNAP_CB, C.c_void_p, C.POINTER(EuRunInfo)]
+    L.eu_get_time.argtypes = [H, _dp, C.POINTER(C.c_longlong), _dp]
+    L.eu_totals.argtypes = [H, _dp]
+    L.eu_compute_dt_host.argtypes = [H, _dp, C.c_double, _dp]
+    L.eu_advance_host.argtypes = [H, _dp, _dp, _dp, C.c_double]
+    L.eu_step_host.argtypes = [H, _dp, _dp, C.c_double, C.c_double, C.c_double, _dp]
+    L.eu_time_steps.argtypes = [H, C.c_int, C.c_int, C.POINTER(C.c_float)]
+    L.eu_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    L.eu_host_free.argtypes = [C.c_void_p]
+    L.eu_host_free.restype = None
+    L.eu_device_info.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int)]
+    _lib = L
+    return L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def case_config(name: str, n: int = 1) -> CaseConfig:
+    """get_n_case_config through the C ABI (src/test_cases.cpp:184-195)."""
+    L = load()
+    c = EuCase()
+    rc = L.eu_get_case_config(name.encode(), int(n), C.byref(c))
+    if rc:
+        raise EulerError(rc, L.eu_last_error(None).decode())
+    return CaseConfig(c.nx, c.ny, c.ng, c.x_min, c.x_max, c.y_min, c.y_max, c.cfl, c.t_end)
+
+
+def device_info():
+    L = load()
+    buf = C.create_string_buffer(256)
+    sm = C.c_int(0)
+    rc = L.eu_device_info(buf, 256, C.byref(sm))
+    if rc:
+        raise EulerError(rc, L.eu_last_error(None).decode())
+    return buf.value.decode(), sm.value
+
+
+class PinnedGrid:
+    """A Grid2D-shaped float64 array in page-locked host memory."""
+
+    def __init__(self, nx: int, ny: int):
+        L = load()
+        self.shape = (ny + 4, nx + 4, 4)
+        nbytes = 8 * int(np.prod(self.shape))
+        self._ptr = C.c_void_p()
+        rc = L.eu_host_alloc(nbytes, C.byref(self._ptr))
+        if rc:
+            raise EulerError(rc, L.eu_last_error(None).decode())
+        buf = (C.c_double * (nbytes // 8)).from_address(self._ptr.value)
+        self.array = np.frombuffer(buf, dtype=np.float64).reshape(self.shape)
+
+    def __del__(self):
+        if getattr(self, "_ptr", None) and self._ptr.value and _lib is not None:
+            self.array = None
+            _lib.eu_host_free(self._ptr)
+            self._ptr = None
+
+
+class Solver:
+    """One device-resident grid (a handle of the C ABI)."""
+
+    def __init__(self, cfg: CaseConfig, precision="fp64", solver="hllc", bc=(0, 0, 0, 0)):
+        L = load()
+        self.cfg = cfg
+        self.precision = precision
+        self.solver = solver
+        self.bc = tuple(int(b) for b in bc)
+        c = EuCase(cfg.nx, cfg.ny, cfg.ng, cfg.x_min, cfg.x_max, cfg.y_min, cfg.y_max, cfg.cfl, cfg.t_end)
+        b4 = (C.c_int * 4)(*self.bc)
+        h = C.c_void_p()
+        prec = FP32 if precision in ("fp32", FP32) else FP64
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        rc = L.eu_create(C.byref(c), prec, s, 0, b4, C.byref(h))
+        if rc:
+            raise EulerError(rc, L.eu_last_error(None).decode())
+        self._h = h
+        self._L = L
+        self.shape = (cfg.ny + 4, cfg.nx + 4, 4)
+
+    @classmethod
+    def for_problem(cls, prob: Problem, precision="fp64", solver="hllc"):
+        s = cls(prob.cfg, precision, solver, prob.bc)
+        s.init(prob)
+        return s
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.eu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            raise EulerError(rc, self._L.eu_last_error(self._h).decode())
+
+    # -- setup --------------------------------------------------------------
+    def init(self, prob: Problem):
+        p = prob.params
+        if isinstance(p, BlastParams):
+            self._check(self._L.eu_init_blast(self._h, p.cx, p.cy, p.r, p.rho_in, p.p_in, p.rho_out, p.p_out))
+        elif isinstance(p, ShockBubbleParams):
+            self._check(self._L.eu_init_shock_bubble(self._h, p.rho0, p.p0, p.mach, p.shock_x, p.bub_cx,
+                                                     p.bub_cy, p.bub_r, p.rho_bubble))
+        else:
+            raise TypeError(type(p))
+
+    def init_reference_case(self, name: str):
+        self._check(self._L.eu_init_reference_case(self._h, name.encode()))
+
+    # -- state ---------------------------------------------------------------
+    def upload(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.shape == self.shape, (U.shape, self.shape)
+        self._check(self._L.eu_upload_aos(self._h, _p(U)))
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.shape) if out is None else out
+        self._check(self._L.eu_download_aos(self._h, _p(out)))
+        return out
+
+    def totals(self) -> np.ndarray:
+        out = np.zeros(4)
+        self._check(self._L.eu_totals(self._h, _p(out)))
+        return out
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_longlong()
+        dt = C.c_double()
+        self._check(self._L.eu_get_time(self._h, C.byref(t), C.byref(n), C.byref(dt)))
+        return t.value, n.value, dt.value
+
+    # -- hot path ------------------------------------------------------------
+    def compute_dt(self, cfl: float | None = None) -> float:
+        dt = C.c_double()
+        self._check(self._L.eu_compute_dt(self._h, self.cfg.cfl if cfl is None else cfl, C.byref(dt)))
+        return dt.value
+
+    def advance(self, dt: float):
+        self._check(self._L.eu_advance(self._h, float(dt)))
+
+    def step_n(self, n: int, dts=None):
+        if dts is None:
+            self._check(self._L.eu_step_n(self._h, int(n), None))
+        else:
+            d = np.ascontiguousarray(dts, dtype=np.float64)
+            assert len(d) >= n
+            self._check(self._L.eu_step_n(self._h, int(n), _p(d)))
+
+    def run(self, t_end: float | None = None, nsnap: int = 0, callback=None):
+        """Device-resident time loop; callback(k, step, t, grid) per snapshot."""
+        t_end = self.cfg.t_end if t_end is None else t_end
+        info = EuRunInfo()
+
+        def _cb(user, k, step, t, aos, nx, ny):
+            arr = np.ctypeslib.as_array(aos, shape=self.shape).copy()
+            try:
+                return int(bool(callback(k, step, t, arr)))
+            except Exception:  # noqa: BLE001 - a raising callback aborts the run
+                return 1
+
+        cb = SNAP_CB(_cb) if callback is not None else SNAP_CB()
+        self._check(self._L.eu_run(self._h, float(t_end), int(nsnap), cb, None, C.byref(info)))
+        return dict(t=info.t, steps=info.steps, status=info.status, snapshots=info.nsnap_written)
+
+    # -- drop-in calls on host grids ----------------------------------------
+    def compute_dt_host(self, U: np.ndarray, cfl: float) -> float:
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        dt = C.c_double()
+        self._check(self._L.eu_compute_dt_host(self._h, _p(U), cfl, C.byref(dt)))
+        return dt.value
+
+    def advance_host(self, Uold: np.ndarray, dt: float, want_tmp=True):
+        Uold = np.ascontiguousarray(Uold, dtype=np.float64)
+        Unew = np.empty(self.shape)
+        Utmp = np.empty(self.shape) if want_tmp else None
+        self._check(self._L.eu_advance_host(self._h, _p(Uold), _p(Utmp) if want_tmp else None, _p(Unew),
+                                            float(dt)))
+        return Utmp, Unew
+
+    def step_host(self, U: np.ndarray, Unext: np.ndarray, cfl: float, t: float, t_end: float) -> float:
+        dt = C.c_double()
+        self._check(self._L.eu_step_host(self._h, _p(U), _p(Unext), cfl, t, t_end, C.byref(dt)))
+        return dt.value
+
+    # -- measurement ---------------------------------------------------------
+    def time_steps(self, nsteps: int, use_graph=True):
+        ms = (C.c_float * 3)()
+        self._check(self._L.eu_time_steps(self._h, int(nsteps), int(bool(use_graph)), ms))
+        return float(ms[0]), float(ms[1]), float(ms[2])

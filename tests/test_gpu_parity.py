@@ -1,0 +1,183 @@
+"""FP64 CUDA path vs the CPU oracle (restatement of the reference solver) on
+the same inputs, through the C ABI.  Tolerances: the spec bar for the
+FP64 drop-in is <= 1e-10 L1 (mean absolute difference over interior cells)
+in density at t_end; single steps are held to 1e-12 relative."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Grid, Oracle
+
+pytestmark = pytest.mark.gpu
+SOLVERS = ("hll", "hllc", "exact", "force")
+
+
+@pytest.fixture(scope="module")
+def E():
+    import large_sys_eq_opt_gb300.euler2d as E
+    E.load()
+    return E
+
+
+def interior(U):
+    return U[2:-2, 2:-2]
+
+
+def l1(a, b):
+    return float(np.mean(np.abs(a - b)))
+
+
+def cfg_of(g: Grid, cfl=0.8, t_end=0.25):
+    from large_sys_eq_opt_gb300.cases import CaseConfig
+    return CaseConfig(g.nx, g.ny, 2, g.x_min, g.x_max, g.y_min, g.y_max, cfl, t_end)
+
+
+def bc_of(g: Grid):
+    return tuple(0 if b in ("transmissive", 0) else 1 for b in g.bc)
+
+
+def test_device_initial_states_match_oracle(E, port):
+    g = Grid(256, 256, 0.0, 2.0, 0.0, 2.0)
+    with E.Solver(cfg_of(g), "fp64", "hllc") as s:
+        s._check(s._L.eu_init_blast(s._h, 1.0, 1.0, 0.4, 1.0, 1.0, 0.125, 0.1))
+        got = s.download()
+    assert np.array_equal(interior(got), interior(port.init_blast(g)))
+    g = Grid(1000, 396, 0.0, 0.225, 0.0, 0.089)
+    with E.Solver(cfg_of(g), "fp64", "hllc") as s:
+        s._check(s._L.eu_init_shock_bubble(s._h, 1.0, 1.0, 1.22, 0.005, 0.035, 0.0445, 0.025, 0.138))
+        got = s.download()
+    assert np.array_equal(interior(got), interior(port.init_shock_bubble(g)))
+
+
+def test_upload_download_roundtrip(E, port):
+    g = Grid(37, 23, 0.0, 1.0, 0.0, 1.0)
+    U = port.init_blast(g, cx=0.5, cy=0.5, r=0.2)
+    port.apply_boundary(U, g)
+    with E.Solver(cfg_of(g), "fp64", "hll") as s:
+        s.upload(U)
+        assert np.array_equal(s.download(), U)
+
+
+def test_compute_dt_matches_oracle(E, port):
+    g = Grid(256, 256, 0.0, 2.0, 0.0, 2.0)
+    U = port.init_blast(g)
+    with E.Solver(cfg_of(g), "fp64", "hllc") as s:
+        s.upload(U)
+        dt = s.compute_dt(0.8)
+    ref = port.compute_dt(U, g, 0.8)
+    assert abs(dt - ref) <= 1e-15 * ref
+
+
+@pytest.mark.parametrize("solver", SOLVERS)
+def test_single_step_golden_cases(E, golden_dir, solver):
+    d = np.load(os.path.join(golden_dir, "step_cases.npz"))
+    names = sorted({k.split("/")[0] for k in d.files})
+    for name in names:
+        geom = d[f"{name}/geom"]
+        g = Grid(int(geom[0]), int(geom[1]), *geom[2:])
+        U = np.ascontiguousarray(d[f"{name}/U"])
+        dt = float(d[f"{name}/dt"][0])
+        with E.Solver(cfg_of(g), "fp64", solver) as s:
+            Utmp, Unew = s.advance_host(U, dt)
+        for lbl, got, ref in (("Utmp", Utmp, d[f"{name}/{solver}/Utmp"]), ("Unew", Unew, d[f"{name}/{solver}/Unew"])):
+            scale = np.maximum(np.abs(ref), 1.0)
+            err = float(np.max(np.abs(got - ref) / scale))
+            assert err <= 1e-12, (name, solver, lbl, err)
+
+
+@pytest.mark.parametrize("solver", SOLVERS)
+def test_blast256_run_to_t_end(E, port, solver):
+    """BASELINE configuration 0 geometry: 256^2 blast, CFL 0.8, t_end 0.25, 5 snapshots."""
+    g = Grid(256, 256, 0.0, 2.0, 0.0, 2.0)
+    U = port.init_blast(g)
+    ref = port.run(U, g, 0.8, 0.25, solver, nsnap=5, want_snapshots=True)
+    snaps = {}
+    with E.Solver(cfg_of(g), "fp64", solver) as s:
+        s._check(s._L.eu_init_blast(s._h, 1.0, 1.0, 0.4, 1.0, 1.0, 0.125, 0.1))
+        info = s.run(0.25, nsnap=5, callback=lambda k, step, t, A: snaps.__setitem__(k, (step, t, A)))
+        got = s.download()
+    assert info["steps"] == ref["steps"]
+    assert abs(info["t"] - ref["t"]) <= 1e-15
+    assert sorted(snaps) == [1, 2, 3, 4, 5]
+    for k in range(5):
+        step, t, A = snaps[k + 1]
+        assert step == ref["snap_step"][k]
+        assert abs(t - ref["snap_t"][k]) <= 1e-14
+        assert l1(interior(A)[..., 0], interior(ref["snapshots"][k])[..., 0]) <= 1e-10
+    assert l1(interior(got)[..., 0], interior(U)[..., 0]) <= 1e-10
+
+
+@pytest.mark.parametrize("solver", ("hllc", "exact"))
+def test_reflective_shock_bubble(E, port, solver):
+    """BASELINE configuration 1 (1000x396, reflective y), first 0.02 of time."""
+    g = Grid(1000, 396, 0.0, 0.225, 0.0, 0.089, bc=("transmissive", "transmissive", "reflective", "reflective"))
+    U = port.init_shock_bubble(g)
+    ref = port.run(U, g, 0.8, 0.02, solver)
+    with E.Solver(cfg_of(g, 0.8, 0.02), "fp64", solver, bc=bc_of(g)) as s:
+        s._check(s._L.eu_init_shock_bubble(s._h, 1.0, 1.0, 1.22, 0.005, 0.035, 0.0445, 0.025, 0.138))
+        info = s.run(0.02)
+        got = s.download()
+    assert info["steps"] == ref["steps"]
+    assert l1(interior(got)[..., 0], interior(U)[..., 0]) <= 1e-10
+
+
+@pytest.mark.parametrize("shape", [(17, 13), (1, 24), (24, 1), (130, 5), (5, 131)])
+def test_odd_sizes_multi_step(E, port, shape):
+    nx, ny = shape
+    g = Grid(nx, ny, 0.0, 1.0, 0.0, 1.0)
+    U = port.init_blast(g, cx=0.3, cy=0.6, r=0.25, rho_in=1.0, p_in=2.0, rho_out=0.3, p_out=0.2)
+    V = U.copy()
+    ref = port.run(V, g, 0.8, 0.1, "hllc", max_steps=12)
+    with E.Solver(cfg_of(g, 0.8, 0.1), "fp64", "hllc") as s:
+        s.upload(U)
+        info = s.run(0.1)
+        assert info["steps"] >= ref["steps"]
+    for _ in range(1):
+        with E.Solver(cfg_of(g, 0.8, 0.1), "fp64", "hllc") as s:
+            s.upload(U)
+            for dt in ref["dts"]:
+                s.advance(dt)
+            got = s.download()
+        err = float(np.max(np.abs(interior(got) - interior(V)) / np.maximum(np.abs(interior(V)), 1.0)))
+        assert err <= 1e-11, (shape, err)
+
+
+def test_fp32_blast256_error_vs_fp64(E, port):
+    g = Grid(256, 256, 0.0, 2.0, 0.0, 2.0)
+    U = port.init_blast(g)
+    port.run(U, g, 0.8, 0.25, "hllc")
+    with E.Solver(cfg_of(g), "fp32", "hllc") as s:
+        s._check(s._L.eu_init_blast(s._h, 1.0, 1.0, 0.4, 1.0, 1.0, 0.125, 0.1))
+        s.run(0.25)
+        got = s.download()
+    e = l1(interior(got)[..., 0], interior(U)[..., 0])
+    print(f"FP32 HLLC blast256 L1(rho) vs FP64 oracle = {e:.3e}")
+    assert e <= 1e-5
+
+
+def test_graph_steps_match_single_steps(E, port):
+    g = Grid(200, 150, 0.0, 2.0, 0.0, 1.5)
+    from large_sys_eq_opt_gb300.cases import CaseConfig
+    with E.Solver(cfg_of(g), "fp64", "hllc") as a, E.Solver(cfg_of(g), "fp64", "hllc") as b:
+        for s in (a, b):
+            s._check(s._L.eu_init_blast(s._h, 1.0, 0.75, 0.3, 1.0, 1.0, 0.125, 0.1))
+        dts = []
+        for _ in range(9):
+            dt = a.compute_dt(0.8)
+            a.advance(dt)
+            dts.append(dt)
+        b.step_n(9, dts)
+        assert np.array_equal(a.download(), b.download())
+        b.step_n(5)
+        t, n, _ = b.time()
+        assert n == 14
+
+
+def test_nonphysical_state_is_reported(E):
+    g = Grid(32, 32)
+    with E.Solver(cfg_of(g), "fp64", "hllc") as s:
+        s.upload(np.zeros((36, 36, 4)))
+        with pytest.raises(E.EulerError) as ei:
+            s.compute_dt(0.8)
+        assert ei.value.code == 4

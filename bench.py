@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Throughput of the MUSCL-Hancock split step on one GB300 (or N replicas).
+
+Metric (the benchmark spec): cell-updates/s, FP32 vs FP64 at the stated L1 error
+vs FP64.  Workload: the cylindrical blast (domain [0,2]^2, r=0.4 at (1,1),
+rho/p 1/1 inside, 0.125/0.1 outside, transmissive, CFL 0.8) on an 8192^2
+grid, HLLC, minmod; synthetic initial state evaluated on the device.
+
+  value  : FP32 HLLC cell-updates/s, state resident in HBM, K steps replayed
+           from one CUDA graph (dt from the fused device reduction), timed
+           with CUDA events on the library's stream.
+  e2e    : the same metric through the drop-in C-ABI call on HOST grids
+           (eu_step_host: H2D of the Grid2D AoS state, dt, step, D2H of the
+           new state every step, pinned buffers).
+  roofline: dominant sweep kernel, algorithmic bytes (read 4 + write 4
+           fields per cell per sweep) / average launch time, against the
+           measured HBM copy bandwidth.
+  cpu_baseline: the CPU oracle (C restatement of the reference solver, FP64,
+           OpenMP over all host cores) on a bounded sample of the workload.
+
+Multi-GPU: the path is run as independent replicas (one grid per rank, no
+collective on the data path); value is the sum over ranks, timing the max.
+`--impl reference` times the reference algorithm's CPU implementation (the
+oracle port; the reference sources are not available on the GPU host) on the
+host cores and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s FP32 vs FP64 at stated L1 err vs FP64; adjoint/forward time ratio"
+UNIT = "cell-updates/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--n", type=int, default=8192, help="grid is n x n")
+    ap.add_argument("--solver", default="hllc", choices=("hll", "hllc", "exact", "force"))
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            td.init_process_group(backend=backend)
+            self.td, self.torch = td, torch
+            self.backend = backend
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(key: str):
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+    recorded from ncu in profiles/*.md as `traffic[<key>] = <bytes>`."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(d, fn)):
+            line = line.strip().strip("`")
+            if line.startswith(f"traffic[{key}]"):
+                try:
+                    return float(line.split("=")[1].split()[0])
+                except (IndexError, ValueError):
+                    pass
+    return None
+
+
+def cpu_port_rate(n: int, solver: str, seconds: float, max_steps: int | None = None):
+    """Oracle port (C restatement of the reference CPU solver, OpenMP on every
+    host core) on the n x n blast: full-size split steps (BC, compute_dt,
+    advance_second_order) until `seconds` of work or max_steps."""
+    from oracle import oracle as O
+    O.build(reference=False)
+    P = O.Oracle("port")
+    threads = os.cpu_count() or 1
+    P.set_threads(threads)
+    g = O.Grid(n, n, 0.0, 2.0, 0.0, 2.0)
+    U = P.init_blast(g)
+    P.run(U, g, 0.8, 1e30, solver, max_steps=1)          # warm-up step
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        P.run(U, g, 0.8, 1e30, solver, max_steps=1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or (max_steps and steps >= max_steps):
+            break
+    rate = n * n * steps / el
+    return rate, threads, steps, el
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    steps_cap = max(1, min(args.steps, 20))
+    rate, threads, steps, el = cpu_port_rate(args.n, args.solver, seconds=1e9, max_steps=steps_cap)
+    sample = (f"{steps} full {args.n}x{args.n} FP64 {args.solver.upper()} split steps (BC + compute_dt + "
+              f"advance_second_order) after 1 warm-up step, {el:.1f} s on {threads} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"blast_{args.n}x{args.n}_{args.solver}", "nx": args.n, "ny": args.n,
+                   "solver": args.solver, "precision": "fp64 (the reference has no FP32 path)"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, dist: Dist):
+    import numpy as np
+
+    import large_sys_eq_opt_gb300.euler2d as E
+    from large_sys_eq_opt_gb300.cases import blast_large
+
+    E.set_device(dist.local)
+    n, K, W = args.n, args.steps, args.warmup
+    prob = blast_large(n)
+    cells = n * n
+    peak, peak_kind = measured_peaks()
+    out = {}
+
+    # ---- FP32 device-resident throughput (the headline) -------------------
+    s32 = E.Solver.for_problem(prob, "fp32", args.solver)
+    s32.time_steps(W)
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        tot, tx, ty = s32.time_steps(K)
+    dist.barrier()
+    tmax = dist.max(tot)
+    value = cells * K * dist.ws / (tmax / 1e3)
+    esz = 4
+    bytes_per_launch = cells * 8 * esz
+    dom, tdom = ("sweep_x", tx) if tx >= ty else ("sweep_y", ty)
+    achieved = bytes_per_launch / (tdom / K / 1e3) / 1e9
+    traffic = profiled_traffic(f"fp32_{args.solver}_{dom}_{n}")
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "traffic": traffic, "kernel": dom,
+                       "peak_source": f"{peak_kind} hbm_gbs",
+                       "per_kernel_ms": {"sweep_x": tx / K, "sweep_y": ty / K},
+                       "algorithmic_bytes_per_launch": bytes_per_launch}
+    out["clocks"] = clk.summary()
+    s32.close()
+
+    # ---- FP64 throughput + FP32-vs-FP64 error at the final step -----------
+    if not args.skip_fp64:
+        s64 = E.Solver.for_problem(prob, "fp64", args.solver)
+        s64.set_dt_log(W + K)
+        s64.time_steps(W)
+        tot64, tx64, ty64 = s64.time_steps(K)
+        v64 = cells * K * dist.ws / (dist.max(tot64) / 1e3)
+        dts = s64.dt_log(W + K)
+        ref = s64.download()
+        s64.close()
+        e32 = E.Solver.for_problem(prob, "fp32", args.solver)
+        e32.step_n(W + K, dts)
+        got = e32.download()
+        e32.close()
+
+        def pres(A):
+            r, mu, mv, en = (A[2:-2, 2:-2, k] for k in range(4))
+            return 0.3999999999999999 * (en - 0.5 * (mu * mu + mv * mv) / r)
+
+        drho = np.abs(got[2:-2, 2:-2, 0] - ref[2:-2, 2:-2, 0])
+        dp = np.abs(pres(got) - pres(ref))
+        out["fp64"] = {"value": v64, "ms_per_step": tot64 / K,
+                       "per_kernel_ms": {"sweep_x": tx64 / K, "sweep_y": ty64 / K}}
+        out["fp32_vs_fp64"] = {"speedup": value / v64, "steps": W + K, "dt": "FP64 dt sequence replayed",
+                               "l1_rho": float(drho.mean()), "linf_rho": float(drho.max()),
+                               "l1_p": float(dp.mean()), "linf_p": float(dp.max())}
+        del got, ref, drho, dp
+
+    # ---- e2e through the drop-in call on host grids -----------------------
+    if not args.skip_e2e:
+        se = E.Solver.for_problem(prob, "fp32", args.solver)
+        A = E.PinnedGrid(n, n)
+        B = E.PinnedGrid(n, n)
+        se.download(A.array)
+        ke, t, t_end = 3, 0.0, 1e30
+        t += se.step_host(A.array, B.array, 0.8, t, t_end)   # warm-up
+        dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(ke):
+            src, dst = (B, A) if k % 2 == 0 else (A, B)
+            t += se.step_host(src.array, dst.array, 0.8, t, t_end)
+        el = dist.max(time.perf_counter() - t0)
+        aos = (n + 4) * (n + 4) * 32
+        out["e2e"] = {"value": cells * ke * dist.ws / el, "unit": UNIT, "h2d_bytes_per_step": aos,
+                      "d2h_bytes_per_step": aos, "steps": ke,
+                      "call": "eu_step_host (Grid2D AoS in, BC + compute_dt + advance_second_order, AoS out)"}
+        se.close()
+        del A, B
+
+    # ---- CPU baseline (oracle port on the host cores) ---------------------
+    if dist.rank == 0 and dist.ws == 1 and not args.skip_cpu:
+        rate, threads, steps, el = cpu_port_rate(n, args.solver, args.cpu_seconds)
+        out["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} full {n}x{n} FP64 {args.solver.upper()} split steps of the oracle port "
+                      f"(OpenMP, {threads} threads) after 1 warm-up step, {el:.1f} s"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": K, "warmup": W,
+            "ms_per_step": tmax / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"blast_{n}x{n}_{args.solver}_fp32", "nx": n, "ny": n, "solver": args.solver,
+                       "limiter": "minmod", "cfl": 0.8, "precision": "fp32 (FP64 pressure recovery under "
+                       "cancellation, FP64 exact-solver Newton)", "graph": f"{K} steps in one CUDA graph",
+                       "l2": "inputs larger than L2 (1.07 GB per FP32 state buffer vs 126 MB L2)",
+                       "parallelism": f"replicas x{dist.ws}"},
+            "gpu_launches": 2 * K,
+            "adjoint_forward_ratio": None,
+        }
+        line.update(out)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

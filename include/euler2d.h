@@ -127,6 +127,13 @@ int eu_step_n(eu_handle* h, long long n, const double* dts);
 int eu_run(eu_handle* h, double t_end, int nsnap, eu_snapshot_cb cb, void* user, eu_run_info* info);
 /* Current time, completed steps and the dt the next step would use. */
 int eu_get_time(eu_handle* h, double* t, long long* steps, double* dt_next);
+/* apply_transmissive_boundary (head/cpu/boundary_cpu.hpp:5-37) with the
+ * handle's per-side rule, on the device state. */
+int eu_apply_boundary(eu_handle* h);
+/* Record the dt of every step (indexed by the handle's step counter; eu_run
+ * restarts it at 0) into a device log of `capacity` entries; 0 disables. */
+int eu_set_dt_log(eu_handle* h, long long capacity);
+int eu_get_dt_log(eu_handle* h, double* out, long long n);
 /* FP64 totals of rho, rhou, rhov, E over the interior (conserved audit). */
 int eu_totals(eu_handle* h, double out[4]);
 
@@ -151,6 +158,8 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]);
 /* Pinned host memory for zero-staging transfers. */
 int eu_host_alloc(size_t bytes, void** p);
 void eu_host_free(void* p);
+/* Device used by handles created afterwards on the calling thread. */
+int eu_set_device(int device);
 /* Name of device 0 and its SM count, for logs. */
 int eu_device_info(char* name, int len, int* sm_count);
 

@@ -83,6 +83,8 @@ struct eu_handle {
     int snap_cap = 0;
     double* d_frozen = nullptr;
     long long frozen_cap = 0;
+    double* d_dtlog = nullptr;
+    long long dtlog_cap = 0;
     CUtensorMap tm_x[2];
     CUtensorMap tm_y;
     SweepKernels K{};
@@ -239,6 +241,11 @@ cudaError_t unpack_tmp(eu_handle* h, double* d_aos) {
     return launch_unpack_aos<double>(planes_t<double>(h), 4, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
 }
 
+cudaError_t fill_ghosts(eu_handle* h, int b) {
+    if (h->prec == EU_FP32) return launch_fill_ghosts<float>(planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->bc, h->st);
+    return launch_fill_ghosts<double>(planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->bc, h->st);
+}
+
 cudaError_t pack_state(eu_handle* h, int b, const double* d_aos) {
     if (h->prec == EU_FP32) return launch_pack_aos<float>(d_aos, planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->st);
     return launch_pack_aos<double>(d_aos, planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->st);
@@ -257,6 +264,8 @@ void ctl_reset(eu_handle* h, int mode, double t_end, long long max_steps) {
     c.mode = mode;
     c.max_steps = max_steps;
     c.cur = h->cur;
+    c.dt_log = h->d_dtlog;
+    c.dt_log_cap = h->dtlog_cap;
 }
 
 int ctl_push(eu_handle* h) {
@@ -467,6 +476,7 @@ void eu_destroy(eu_handle* h) {
     cudaFreeHost(h->h_tot);
     cudaFree(h->snap);
     cudaFree(h->d_frozen);
+    cudaFree(h->d_dtlog);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }
@@ -606,6 +616,7 @@ int eu_step_n(eu_handle* h, long long n, const double* dts) {
     }
     int rc = ctl_push(h);
     if (rc) return rc;
+    EU_CUDA(h, fill_ghosts(h, h->cur));  // scripts/cpu/main_cpu.cpp:222
     if (!dts) EU_CUDA(h, launch_dt(h, h->cur));
     const int K = h->gsteps;
     const long long reps = (n + K - 1) / K;
@@ -635,6 +646,7 @@ int eu_run(eu_handle* h, double t_end, int nsnap, eu_snapshot_cb cb, void* user,
     c.nsnap = want ? nsnap : 0;  // without storage no snapshot is ever requested
     for (int k = 0; k < nsnap; ++k) c.snap_target[k] = t_end * (double)(k + 1) / (double)nsnap;  // main_cpu.cpp:210-215
     if ((rc = ctl_push(h))) return rc;
+    EU_CUDA(h, fill_ghosts(h, h->cur));  // scripts/cpu/main_cpu.cpp:222
     EU_CUDA(h, launch_dt(h, h->cur));
     if ((rc = ctl_pull_sync(h))) return rc;
     int delivered = 0;
@@ -735,6 +747,7 @@ int eu_step_host(eu_handle* h, const double* U, double* Unext, double cfl, doubl
     c.cfl_dmin = cfl * std::min(h->dx, h->dy);
     c.t = t;
     if ((rc = ctl_push(h))) return rc;
+    EU_CUDA(h, fill_ghosts(h, h->cur));         // apply_transmissive_boundary(U)
     EU_CUDA(h, launch_dt(h, h->cur));           // dt = compute_dt(U), clipped to t_end - t
     EU_CUDA(h, cudaMemcpyAsync(&h->hctl->dt, &h->ctl->dt, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     EU_CUDA(h, launch_step(h, h->cur));
@@ -758,6 +771,7 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
     c.step = s0;
     int rc = ctl_push(h);
     if (rc) return rc;
+    EU_CUDA(h, fill_ghosts(h, h->cur));
     EU_CUDA(h, launch_dt(h, h->cur));
     std::vector<cudaEvent_t> ev(2 * (size_t)nsteps + 1, nullptr);
     for (auto& e : ev) EU_CUDA(h, cudaEventCreate(&e));
@@ -810,6 +824,42 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
     rc = ctl_pull_sync(h);
     if (rc) return rc;
     return status_code(h);
+}
+
+int eu_apply_boundary(eu_handle* h) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    EU_CUDA(h, fill_ghosts(h, h->cur));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_set_dt_log(eu_handle* h, long long capacity) {
+    if (!h || capacity < 0) return fail(h, EU_ERR_INVALID, "bad argument");
+    cudaFree(h->d_dtlog);
+    h->d_dtlog = nullptr;
+    h->dtlog_cap = 0;
+    if (capacity > 0) {
+        EU_CUDA(h, cudaMalloc(&h->d_dtlog, sizeof(double) * (size_t)capacity));
+        EU_CUDA(h, cudaMemsetAsync(h->d_dtlog, 0, sizeof(double) * (size_t)capacity, h->st));
+        h->dtlog_cap = capacity;
+    }
+    h->hctl->dt_log = h->d_dtlog;
+    h->hctl->dt_log_cap = h->dtlog_cap;
+    return ctl_push(h);
+}
+
+int eu_get_dt_log(eu_handle* h, double* out, long long n) {
+    if (!h || !out || n < 0 || n > h->dtlog_cap) return fail(h, EU_ERR_INVALID, "bad argument");
+    if (n == 0) return EU_OK;
+    EU_CUDA(h, cudaMemcpyAsync(out, h->d_dtlog, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_set_device(int device) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+    return EU_OK;
 }
 
 int eu_host_alloc(size_t bytes, void** p) {

@@ -61,6 +61,28 @@ __global__ void unpack_aos_kernel(Planes<T> P, int coff, int nx, int ny, int4 bc
     }
 }
 
+// Ghost frame of an S buffer from its interior (apply_transmissive_boundary,
+// head/cpu/boundary_cpu.hpp:5-37, with the per-side rule).  Ghosts read only
+// interior cells, so every ghost is written independently.
+template <class T>
+__global__ void fill_ghosts_kernel(Planes<T> P, int nx, int ny, int4 bc) {
+    const long long tnx = nx + 4, total = tnx * (ny + 4);
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(idx / tnx), c = (int)(idx - (long long)r * tnx);
+        if (r >= 2 && r < ny + 2 && c >= 2 && c < nx + 2) continue;
+        bool fx, fy;
+        const int si = ghost_src(c, nx, bc.x, bc.y, fx);
+        const int sj = ghost_src(r, ny, bc.z, bc.w, fy);
+        const T* q = P.base + (long long)(sj + 2) * P.pitch + (si + 2);
+        T* o = P.base + (long long)r * P.pitch + c;
+        o[0] = q[0];
+        o[P.plane] = fx ? -q[P.plane] : q[P.plane];
+        o[2 * P.plane] = fy ? -q[2 * P.plane] : q[2 * P.plane];
+        o[3 * P.plane] = q[3 * P.plane];
+    }
+}
+
 // Interior SoA snapshot [f][ny][nx] -> AoS double grid with ghosts.
 template <class T>
 __global__ void unpack_snapshot_kernel(const T* __restrict__ s, long long plane, int nx, int ny, int4 bc,
@@ -236,6 +258,12 @@ cudaError_t launch_unpack_aos(Planes<T> P, int coff, int nx, int ny, const int b
     return cudaGetLastError();
 }
 template <class T>
+cudaError_t launch_fill_ghosts(Planes<T> P, int nx, int ny, const int bc[4], cudaStream_t s) {
+    const long long n = (long long)(nx + 4) * (ny + 4);
+    fill_ghosts_kernel<T><<<grid_for(n, 256), 256, 0, s>>>(P, nx, ny, make_int4(bc[0], bc[1], bc[2], bc[3]));
+    return cudaGetLastError();
+}
+template <class T>
 cudaError_t launch_unpack_snapshot(const T* snap, long long plane, int nx, int ny, const int bc[4],
                                    double* aos, cudaStream_t s) {
     const long long n = (long long)(nx + 4) * (ny + 4);
@@ -276,6 +304,7 @@ cudaError_t launch_totals(Planes<T> P, int coff, int nx, int ny, double* part, i
     template cudaError_t launch_pack_aos<T>(const double*, Planes<T>, int, int, cudaStream_t);     \
     template cudaError_t launch_unpack_aos<T>(Planes<T>, int, int, int, const int*, double*,       \
                                               cudaStream_t);                                         \
+    template cudaError_t launch_fill_ghosts<T>(Planes<T>, int, int, const int*, cudaStream_t);     \
     template cudaError_t launch_unpack_snapshot<T>(const T*, long long, int, int, const int*,      \
                                                    double*, cudaStream_t);                           \
     template cudaError_t launch_init_blast<T>(Planes<T>, GridGeom, BlastDesc, cudaStream_t);        \

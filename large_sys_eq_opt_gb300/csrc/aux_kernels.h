@@ -18,6 +18,7 @@ struct ShockBubbleDesc {
 template <class T> cudaError_t launch_pack_aos(const double* aos, Planes<T> P, int nx, int ny, cudaStream_t s);
 template <class T>
 cudaError_t launch_unpack_aos(Planes<T> P, int coff, int nx, int ny, const int bc[4], double* aos, cudaStream_t s);
+template <class T> cudaError_t launch_fill_ghosts(Planes<T> P, int nx, int ny, const int bc[4], cudaStream_t s);
 template <class T>
 cudaError_t launch_unpack_snapshot(const T* snap, long long plane, int nx, int ny, const int bc[4], double* aos,
                                    cudaStream_t s);

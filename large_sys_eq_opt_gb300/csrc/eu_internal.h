@@ -21,6 +21,8 @@ struct Ctl {
     double cfl_dmin;     // cfl * min(dx, dy)
     double smax;         // last reduced maximum signal speed (diagnostic)
     const double* frozen;  // frozen dt list (mode kModeFrozen)
+    double* dt_log;        // dt of every completed step (may be null)
+    long long dt_log_cap;
     long long n_frozen;
     long long frozen_base;  // step index of frozen[0]
     long long max_steps; // done once step reaches this

@@ -152,6 +152,7 @@ static __device__ __noinline__ void finalize_step(Ctl* c, int advance, int out_i
     c->smax = smax;
     if (advance) {
         const double t_new = c->t + c->dt;        // scripts/cpu/main_cpu.cpp:241
+        if (c->dt_log && c->step < c->dt_log_cap) c->dt_log[c->step] = c->dt;
         c->t = t_new;
         c->step += 1;
         c->cur = out_index;

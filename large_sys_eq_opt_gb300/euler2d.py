@@ -51,7 +51,8 @@ EXPORTS = (
     "eu_init_reference_case", "eu_init_blast", "eu_init_shock_bubble", "eu_upload_aos",
     "eu_download_aos", "eu_compute_dt", "eu_advance", "eu_step_n", "eu_run", "eu_get_time",
     "eu_totals", "eu_compute_dt_host", "eu_advance_host", "eu_step_host", "eu_time_steps",
-    "eu_host_alloc", "eu_host_free", "eu_device_info",
+    "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
+    "eu_get_dt_log", "eu_set_device",
 )
 
 _lib = None
@@ -100,6 +101,10 @@ def load(path: str = LIB_PATH):
     L.eu_host_free.argtypes = [C.c_void_p]
     L.eu_host_free.restype = None
     L.eu_device_info.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int)]
+    L.eu_apply_boundary.argtypes = [H]
+    L.eu_set_dt_log.argtypes = [H, C.c_longlong]
+    L.eu_get_dt_log.argtypes = [H, _dp, C.c_longlong]
+    L.eu_set_device.argtypes = [C.c_int]
     _lib = L
     return L
 
@@ -116,6 +121,13 @@ def case_config(name: str, n: int = 1) -> CaseConfig:
     if rc:
         raise EulerError(rc, L.eu_last_error(None).decode())
     return CaseConfig(c.nx, c.ny, c.ng, c.x_min, c.x_max, c.y_min, c.y_max, c.cfl, c.t_end)
+
+
+def set_device(device: int):
+    L = load()
+    rc = L.eu_set_device(int(device))
+    if rc:
+        raise EulerError(rc, L.eu_last_error(None).decode())
 
 
 def device_info():
@@ -217,6 +229,17 @@ class Solver:
     def download(self, out: np.ndarray | None = None) -> np.ndarray:
         out = np.empty(self.shape) if out is None else out
         self._check(self._L.eu_download_aos(self._h, _p(out)))
+        return out
+
+    def apply_boundary(self):
+        self._check(self._L.eu_apply_boundary(self._h))
+
+    def set_dt_log(self, capacity: int):
+        self._check(self._L.eu_set_dt_log(self._h, int(capacity)))
+
+    def dt_log(self, n: int) -> np.ndarray:
+        out = np.zeros(int(n))
+        self._check(self._L.eu_get_dt_log(self._h, _p(out), int(n)))
         return out
 
     def totals(self) -> np.ndarray:

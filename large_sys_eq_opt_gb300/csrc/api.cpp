@@ -123,7 +123,7 @@ template <class T> Planes<T> planes_t(const eu_handle* h) {
 }
 
 int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long pitch, long long plane,
-           int box_w, int box_h) {
+           int box_w, int box_h, CUtensorMapSwizzle swz) {
     auto fn = encode_fn();
     if (!fn) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
     const cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)(h->cfg.ny + 4), 4};
@@ -132,7 +132,7 @@ int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long 
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = fn(m, h->prec == EU_FP32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
                           3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return EU_OK;
@@ -143,20 +143,23 @@ int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long 
 // small fraction of the work.
 void plan(eu_handle* h) {
     const int nx = h->cfg.nx, ny = h->cfg.ny;
-    const long long target = (long long)h->sm_count * 24;
-    const int W = 32 * h->K.vec_x;
-    const int max_seg = (nx + W - 1) / W;
-    int nseg = (int)std::min<long long>(std::max<long long>((target + ny - 1) / ny, 1), max_seg);
-    h->seg_x = (int)round_up((nx + nseg - 1) / nseg, W);
-    h->nseg_x = (nx + h->seg_x - 1) / h->seg_x;
-    h->ntasks_x = ny * h->nseg_x;
+    const long long target = (long long)h->sm_count * 32;   // warps: ~2 resident waves
+    // x-sweep: 32 rows per warp, segments of whole boxes along x
+    const int rgroups = (ny + 31) / 32;
+    const int CX = h->K.box_x;
+    const int max_seg = (nx + CX - 1) / CX;
+    int nseg = (int)std::min<long long>(std::max<long long>((target + rgroups - 1) / rgroups, 1), max_seg);
+    int seg = (int)round_up((nx + nseg - 1) / nseg, CX);
+    seg = std::max(seg, (int)std::min<long long>(round_up(nx, CX), 256));  // keep the 4-cell warm-up small
+    h->seg_x = seg;
+    h->nseg_x = (nx + seg - 1) / seg;
+    h->ntasks_x = rgroups * h->nseg_x;
     h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
-
-    const int WY = 32 * h->K.vec_y;
-    const int groups = (nx + h->K.off_y + WY - 1) / WY;
+    // y-sweep: 32 columns per warp, row segments
+    const int groups = (nx + 31) / 32;
     int nsy = (int)std::max<long long>((target + groups - 1) / groups, 1);
     int segy = (ny + nsy - 1) / nsy;
-    segy = std::max(segy, std::min(ny, 64));
+    segy = std::max(segy, std::min(ny, 128));
     h->seg_y = segy;
     h->nseg_y = groups;  // tasks per row segment
     h->ntasks_y = groups * ((ny + segy - 1) / segy);
@@ -446,11 +449,12 @@ int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limite
     ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
     if (ctl_push(h)) { g_err = h->err; return bail(EU_ERR_CUDA); }
     for (int b = 0; b < 2; ++b)
-        if (encode(h, &h->tm_x[b], h->S[b], cfg->nx + 4, h->pitch_s, h->plane_s, 32 * h->K.vec_x, 1)) {
+        if (encode(h, &h->tm_x[b], h->S[b], cfg->nx + 4, h->pitch_s, h->plane_s, h->K.box_x, 32,
+                   CU_TENSOR_MAP_SWIZZLE_32B)) {
             g_err = h->err;
             return bail(EU_ERR_CUDA);
         }
-    if (encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry)) {
+    if (encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE)) {
         g_err = h->err;
         return bail(EU_ERR_CUDA);
     }

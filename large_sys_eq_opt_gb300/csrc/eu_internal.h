@@ -77,10 +77,8 @@ using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const void* args, int
 
 struct SweepKernels {
     SweepLaunch x, y;
-    int vec_x, vec_y;    // cells per lane
-    int off_y;           // interior column of lane 0 in y-sweep group 0 is -off_y
-    int ry;              // rows per y-sweep TMA box
-    int box_w_y;         // y-sweep box width in elements
+    int box_x;           // x-sweep box: box_x columns (32 bytes) x 32 rows, 32-byte swizzle
+    int ry;              // y-sweep box: 32 columns x ry rows
     int stages_x, stages_y;
     int nw;              // warps per CTA
     size_t smem_x, smem_y;

@@ -57,7 +57,7 @@ template <> struct Ar<float> {
     // Approximate reciprocal and square root (max error ~1-2 ulp); the FP32
     // form is judged against FP64 by its L1/Linf error, not bit-for-bit.
     static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
-    static __device__ __forceinline__ float sqrt_(float x) { return __fsqrt_rn(x) ; }
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
     static __device__ __forceinline__ float fmin_(float a, float b) { return fminf(a, b); }
     static __device__ __forceinline__ float fmax_(float a, float b) { return fmaxf(a, b); }
@@ -102,7 +102,7 @@ template <> __device__ __forceinline__ Prim<float> cons_to_prim<float>(const Con
     V.ut = U.mt * V.ir;
     const float kinetic = 0.5f * U.r * (V.un * V.un + V.ut * V.ut);
     V.p = gm1<float>() * (U.e - kinetic);
-    if (2.0f * kinetic > U.e) V.p = pressure_fp64(U.r, U.mn, U.mt, U.e);
+    if (__builtin_expect(2.0f * kinetic > U.e, 0)) V.p = pressure_fp64(U.r, U.mn, U.mt, U.e);
     return V;
 }
 
@@ -152,15 +152,11 @@ template <class T> __device__ __forceinline__ bool physical_recon(const Prim<T>&
 // ---------------------------------------------------------------------------
 // Riemann solvers.  Inputs carry their primitives (V = cons_to_prim(U)).
 // ---------------------------------------------------------------------------
-// head/riemann.hpp:87-129
+// HLL flux given the wave-speed estimates and the physical fluxes
+// (head/riemann.hpp:114-128).
 template <class T>
-__device__ __noinline__ Cons<T> hll_flux(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
-                                         const Prim<T>& VR) {
-    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
-    if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(FL, FR);
-    const T aL = sound_speed(VL), aR = sound_speed(VR);
-    const T SL = Ar<T>::fmin_(VL.un - aL, VR.un - aR);
-    const T SR = Ar<T>::fmax_(VL.un + aL, VR.un + aR);
+__device__ __forceinline__ Cons<T> hll_from(const Cons<T>& UL, const Cons<T>& UR, const Cons<T>& FL,
+                                            const Cons<T>& FR, T SL, T SR) {
     if (SL >= T(0)) return FL;
     if (SR <= T(0)) return FR;
     const T den = SR - SL;
@@ -172,24 +168,38 @@ __device__ __noinline__ Cons<T> hll_flux(const Cons<T>& UL, const Prim<T>& VL, c
                    (SR * FL.e - SL * FR.e + ss * (UR.e - UL.e)) * id};
 }
 
+// head/riemann.hpp:87-129 (Davis wave speeds; central average for
+// non-physical input)
+template <class T>
+__device__ __forceinline__ Cons<T> hll_flux(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
+                                            const Prim<T>& VR) {
+    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(FL, FR);
+    const T aL = sound_speed(VL), aR = sound_speed(VR);
+    const T SL = Ar<T>::fmin_(VL.un - aL, VR.un - aR);
+    const T SR = Ar<T>::fmax_(VL.un + aL, VR.un + aR);
+    return hll_from(UL, UR, FL, FR, SL, SR);
+}
+
 // head/riemann.hpp:135-271
 template <class T>
 __device__ __forceinline__ Cons<T> hllc_flux(const Cons<T>& UL, const Prim<T>& VL,
                                              const Cons<T>& UR, const Prim<T>& VR) {
-    if (!physical_riemann(VL) || !physical_riemann(VR)) return hll_flux(UL, VL, UR, VR);
+    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    // non-physical input: hll_flux, which returns the central average
+    if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(FL, FR);
     const T aL = sound_speed(VL), aR = sound_speed(VR);
     const T unL = VL.un, unR = VR.un;
     const T SL = Ar<T>::fmin_(unL - aL, unR - aR);
     const T SR = Ar<T>::fmax_(unL + aL, unR + aR);
-    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
     if (SL >= T(0)) return FL;
     if (SR <= T(0)) return FR;
     const T qL = VL.r * (SL - unL), qR = VR.r * (SR - unR);
     const T numerator = VR.p - VL.p + qL * unL - qR * unR;
     const T denominator = qL - qR;
-    if (Ar<T>::fabs_(denominator) < T(1.0e-14)) return hll_flux(UL, VL, UR, VR);
     const T Sstar = numerator * Ar<T>::rcp(denominator);
-    if (!Ar<T>::finite(Sstar)) return hll_flux(UL, VL, UR, VR);
+    if (Ar<T>::fabs_(denominator) < T(1.0e-14) || !Ar<T>::finite(Sstar))
+        return hll_from(UL, UR, FL, FR, SL, SR);
     // Upwind side of the contact: one star state, selected without branching.
     const bool left = Sstar >= T(0);
     const Cons<T> U = left ? UL : UR;
@@ -200,17 +210,14 @@ __device__ __forceinline__ Cons<T> hllc_flux(const Cons<T>& UL, const Prim<T>& V
     const T ut = left ? VL.ut : VR.ut;
     const T irho = left ? VL.ir : VR.ir;
     const T S = left ? SL : SR;
-    // hllc_star_state (head/riemann.hpp:135-186)
+    // hllc_star_state (head/riemann.hpp:135-186): falls back to U itself
     const T dS = S - Sstar;
-    Cons<T> Us = U;
-    if (!(Ar<T>::fabs_(dS) < T(1.0e-14))) {
-        const T q = rho * (S - un);
-        const T rho_star = q * Ar<T>::rcp(dS);
-        if (Ar<T>::finite(rho_star) && rho_star > T(0)) {
-            const T E_star = rho_star * (U.e * irho + (Sstar - un) * (Sstar + p * Ar<T>::rcp(q)));
-            if (Ar<T>::finite(E_star)) Us = Cons<T>{rho_star, rho_star * Sstar, rho_star * ut, E_star};
-        }
-    }
+    const T q = rho * (S - un);
+    const T rho_star = q * Ar<T>::rcp(dS);
+    const T E_star = rho_star * (U.e * irho + (Sstar - un) * (Sstar + p * Ar<T>::rcp(q)));
+    const bool ok = !(Ar<T>::fabs_(dS) < T(1.0e-14)) && Ar<T>::finite(rho_star) && rho_star > T(0) &&
+                    Ar<T>::finite(E_star);
+    const Cons<T> Us = ok ? Cons<T>{rho_star, rho_star * Sstar, rho_star * ut, E_star} : U;
     return Cons<T>{F.r + S * (Us.r - U.r), F.mn + S * (Us.mn - U.mn), F.mt + S * (Us.mt - U.mt),
                    F.e + S * (Us.e - U.e)};
 }
@@ -219,11 +226,11 @@ __device__ __forceinline__ Cons<T> hllc_flux(const Cons<T>& UL, const Prim<T>& V
 template <class T>
 __device__ __forceinline__ Cons<T> force_flux(const Cons<T>& UL, const Prim<T>& VL,
                                               const Cons<T>& UR, const Prim<T>& VR) {
-    if (!physical_riemann(VL) || !physical_riemann(VR)) return hll_flux(UL, VL, UR, VR);
-    const T aL = sound_speed(VL), aR = sound_speed(VR);
-    const T alpha = Ar<T>::fmax_(Ar<T>::fabs_(VL.un) + aL, Ar<T>::fabs_(VR.un) + aR);
     const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
     const Cons<T> Fc = c_avg(FL, FR);
+    if (!physical_riemann(VL) || !physical_riemann(VR)) return Fc;   // hll_flux -> central average
+    const T aL = sound_speed(VL), aR = sound_speed(VR);
+    const T alpha = Ar<T>::fmax_(Ar<T>::fabs_(VL.un) + aL, Ar<T>::fabs_(VR.un) + aR);
     if (!Ar<T>::finite(alpha) || alpha <= T(1.0e-14)) return Fc;
     const T ha = T(0.5) * alpha;
     const T hia = T(0.5) * Ar<T>::rcp(alpha);
@@ -323,7 +330,7 @@ __device__ __forceinline__ void exact_sample(const Prim<T>& V, T a, T p_star, T 
 template <class T>
 __device__ __forceinline__ Cons<T> exact_flux(const Cons<T>& UL, const Prim<T>& VL,
                                               const Cons<T>& UR, const Prim<T>& VR) {
-    if (!physical_riemann(VL) || !physical_riemann(VR)) return hll_flux(UL, VL, UR, VR);
+    if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(flux(UL, VL), flux(UR, VR));
     const T aL = sound_speed(VL), aR = sound_speed(VR);
     const PrimD L{(double)VL.r, (double)VL.un, (double)VL.ut, (double)VL.p, (double)aL};
     const PrimD R{(double)VR.r, (double)VR.un, (double)VR.ut, (double)VR.p, (double)aR};
@@ -358,9 +365,12 @@ __device__ __forceinline__ Cons<T> riemann(const Cons<T>& UL, const Prim<T>& VL,
 // ---------------------------------------------------------------------------
 // src/cpu/solver_cpu.cpp:22-99  minmod-limited MUSCL-Hancock reconstruction
 // ---------------------------------------------------------------------------
+// minmod(a, b): 0 when a*b <= 0, else the argument of smaller magnitude
+// (src/cpu/solver_cpu.cpp:22-28); for same-sign arguments min(a,b) (a > 0)
+// or max(a,b) (a < 0) equals copysign(min(|a|,|b|), a) exactly.
 template <class T> __device__ __forceinline__ T minmod(T a, T b) {
-    if (a * b <= T(0)) return T(0);
-    return (a > T(0)) ? Ar<T>::fmin_(a, b) : Ar<T>::fmax_(a, b);
+    const T m = copysign(Ar<T>::fmin_(Ar<T>::fabs_(a), Ar<T>::fabs_(b)), a);
+    return (a * b > T(0)) ? m : T(0);
 }
 
 // Face states of one cell: the half-step-evolved left/right boundary states

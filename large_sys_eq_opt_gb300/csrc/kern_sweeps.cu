@@ -22,33 +22,36 @@ namespace {
 
 #if EU_PREC == 32
 using T = float;
-// x: 4 cells/lane (float4), 4 stages of 128x1x4 boxes.
-// y: 2 cells/lane (float2), boxes of 68 columns x 2 rows x 4 fields, 3 stages.
-constexpr int VX = 4, SX = 4;
-constexpr int VY = 2, RY = 2, OFFY = 2, BWY = 68, SY = 3;
+constexpr int MINB_X = 4, MINB_Y = 4;   // 16 resident warps per SM (<= 128 registers)
 #else
 using T = double;
-// x: 2 cells/lane (double2), 4 stages of 64x1x4 boxes.
-// y: 1 cell/lane, boxes of 36 columns x 2 rows x 4 fields, 3 stages.
-constexpr int VX = 2, SX = 4;
-constexpr int VY = 1, RY = 2, OFFY = 0, BWY = 36, SY = 3;
+constexpr int MINB_X = 2, MINB_Y = 2;
 #endif
+// x: boxes of 32 rows x 32 bytes x 4 fields (4 KB), 3 stages per warp.
+// y: boxes of 32 columns x RY rows x 4 fields, 3 stages per warp.
+constexpr int CX = 32 / sizeof(T);
+constexpr int SX = 3;
+constexpr int RY = 4, SY = 3;
 constexpr int NW = 4;
 constexpr int SOL = EU_SOLVER;
-constexpr size_t kStageX = 4 * 32 * VX * sizeof(T);
-constexpr size_t kStageY = 4 * RY * BWY * sizeof(T);
-constexpr size_t kSmemX = NW * SX * kStageX + NW * SX * sizeof(uint64_t);
-constexpr size_t kSmemY = NW * SY * kStageY + NW * SY * sizeof(uint64_t);
-static_assert(kStageX % 128 == 0 && kStageY % 128 == 0, "stage buffers must stay 128-byte aligned");
+constexpr size_t kStageX = 4 * 32 * CX * sizeof(T);
+constexpr size_t kStageY = 4 * RY * 32 * sizeof(T);
+constexpr size_t kSmemX = 1024 + NW * SX * kStageX + NW * SX * sizeof(uint64_t);
+constexpr size_t kSmemY = 1024 + NW * SY * kStageY + NW * SY * sizeof(uint64_t);
 
 static cudaError_t LAUNCH_X(const CUtensorMap* tm, const void* args, int ctas, cudaStream_t s) {
-    sweep_x_kernel<T, SOL, VX, SX, NW><<<ctas, NW * 32, kSmemX, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
+    auto k = sweep_x_kernel<T, SOL, SX, NW, MINB_X>;
+    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX);
+    if (attr != cudaSuccess) return attr;
+    k<<<ctas, NW * 32, kSmemX, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
 }
 
 static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const void* args, int ctas, cudaStream_t s) {
-    sweep_y_kernel<T, SOL, VY, RY, BWY, OFFY, SY, NW>
-        <<<ctas, NW * 32, kSmemY, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
+    auto k = sweep_y_kernel<T, SOL, RY, SY, NW, MINB_Y>;
+    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
+    if (attr != cudaSuccess) return attr;
+    k<<<ctas, NW * 32, kSmemY, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
 }
 
@@ -58,11 +61,8 @@ SweepKernels EU_NAME(sweep_kernels, EU_PREC, EU_SOLVER)() {
     SweepKernels k;
     k.x = LAUNCH_X;
     k.y = LAUNCH_Y;
-    k.vec_x = VX;
-    k.vec_y = VY;
-    k.off_y = OFFY;
+    k.box_x = CX;
     k.ry = RY;
-    k.box_w_y = BWY;
     k.stages_x = SX;
     k.stages_y = SY;
     k.nw = NW;

@@ -4,24 +4,23 @@
 // Data layout in HBM (SoA planes, 2-cell ghost frame):
 //   state buffers S0/S1 : interior (i, j) at column i+2, row j+2
 //   Utmp                : interior (i, j) at column i+4, row j+2
-// The extra two columns of Utmp absorb the x-sweep's two-cell output lag so
-// that every lane of both sweeps stores whole 16-byte vectors.
+// The x-sweep finalises a cell two cells behind the newest one it reads; the
+// extra two columns of Utmp turn that lag into an aligned 16-byte store.
 //
-// Execution model: every warp is an independent marching unit with its own
-// shared-memory stages and mbarriers.  Lane 0 streams boxes of the input
-// planes into shared memory with TMA (cp.async.bulk.tensor.3d, all four
-// fields in one box) while the warp computes on earlier boxes.  Each lane
-// owns VEC adjacent cells; the stencil state slides through registers along
-// the march direction, so each cell is reconstructed once and each face
-// solved once.  Nothing is written back except the updated cells (and the
-// ghost lines the next sweep reads):
-//   x-sweep : warp marches along one row, W = 32*VEC cells per box; the
-//             neighbour values cross lanes by warp shuffles and cross boxes
-//             through lane 0's carry registers.
-//   y-sweep : warp covers 32*VEC columns and marches up a row segment, RY rows
-//             per box; no shuffles at all.  Its epilogue reduces the maximum
-//             signal speed (warp shuffle max -> one atomic per warp) and the
-//             last warp to finish computes the next dt on the device.
+// Execution model: every lane owns one grid line (a row in the x-sweep, a
+// column in the y-sweep) and marches along it; the 5-cell stencil window
+// (two primitive states, two conserved states, the last face state and the
+// last face flux) slides through registers, so each cell is converted and
+// reconstructed once and each face solved once, with no cross-lane traffic.
+// Every warp is an independent unit with its own shared-memory stages and
+// mbarriers: lane 0 streams the next boxes of all four field planes into
+// shared memory with TMA (cp.async.bulk.tensor.3d) while the warp computes.
+//   x-sweep : 32 rows per warp; boxes of 32 rows x 32 bytes, stored with the
+//             32-byte swizzle so that 16-byte row reads are bank-conflict free.
+//   y-sweep : 32 columns per warp; boxes of 32 columns x RY rows.  Its
+//             epilogue reduces the maximum signal speed (warp shuffle max ->
+//             one atomic per warp) and the last warp to finish computes the
+//             next dt on the device.
 #pragma once
 #include "eu_internal.h"
 #include "euler_numerics.cuh"
@@ -30,40 +29,37 @@
 namespace eu {
 
 // ---------------------------------------------------------------------------
-// warp helpers
+// The marching stencil window of one line
 // ---------------------------------------------------------------------------
-template <class T> __device__ __forceinline__ T shfl_rot(T v, int lane) {
-    return __shfl_sync(0xffffffffu, v, (lane + 31) & 31);
-}
+// push(U_c) takes the next cell c of the line and returns the updated cell
+// c-2: cell c-1 is reconstructed from (c-2, c-1, c) and half-step evolved
+// (src/cpu/solver_cpu.cpp:68-99), the face (c-2 | c-1) is solved
+// (head/riemann.hpp:650-672) and cell c-2 is updated with its two face
+// fluxes (src/cpu/solver_cpu.cpp:452-453, :489-490).
+template <class T, int S> struct Line {
+    Prim<T> Wm2, Wm1;   // primitives of cells c-2, c-1
+    Cons<T> Um2, Um1;   // conserved states of cells c-2, c-1
+    Face<T> Rp;         // evolved right face state of cell c-2
+    Cons<T> Fp;         // flux through face (c-3 | c-2)
 
-// Value held by the owner of the previous cells: lane-1, or for lane 0 the
-// value lane 31 held in the previous box (kept in `carry`).
-template <class T> __device__ __forceinline__ T prev_of(T v, T& carry, int lane) {
-    const T r = shfl_rot(v, lane);
-    const T out = (lane == 0) ? carry : r;
-    carry = r;
-    return out;
-}
-template <class T>
-__device__ __forceinline__ Cons<T> prev_of(const Cons<T>& v, Cons<T>& c, int lane) {
-    return Cons<T>{prev_of(v.r, c.r, lane), prev_of(v.mn, c.mn, lane), prev_of(v.mt, c.mt, lane),
-                   prev_of(v.e, c.e, lane)};
-}
-// Primitive without 1/rho (the reconstruction never reads it).
-template <class T>
-__device__ __forceinline__ Prim<T> prev_prim4(const Prim<T>& v, Prim<T>& c, int lane) {
-    return Prim<T>{prev_of(v.r, c.r, lane), prev_of(v.un, c.un, lane), prev_of(v.ut, c.ut, lane),
-                   prev_of(v.p, c.p, lane), T(0)};
-}
-template <class T>
-__device__ __forceinline__ Face<T> prev_face(const Face<T>& v, Face<T>& c, int lane) {
-    Face<T> o;
-    o.U = prev_of(v.U, c.U, lane);
-    o.V = Prim<T>{prev_of(v.V.r, c.V.r, lane), prev_of(v.V.un, c.V.un, lane),
-                  prev_of(v.V.ut, c.V.ut, lane), prev_of(v.V.p, c.V.p, lane),
-                  prev_of(v.V.ir, c.V.ir, lane)};
-    return o;
-}
+    __device__ __forceinline__ void reset() {
+        Wm2 = Prim<T>{}; Wm1 = Prim<T>{}; Um2 = Cons<T>{}; Um1 = Cons<T>{};
+        Rp = Face<T>{}; Fp = Cons<T>{};
+    }
+
+    __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
+        const Prim<T> W = cons_to_prim(U);
+        Face<T> L, R;
+        reconstruct(Wm2, Wm1, W, hl, L, R);
+        const Cons<T> F = riemann<S>(Rp.U, Rp.V, L.U, L.V);
+        const Cons<T> N{Um2.r - lam * (F.r - Fp.r), Um2.mn - lam * (F.mn - Fp.mn),
+                        Um2.mt - lam * (F.mt - Fp.mt), Um2.e - lam * (F.e - Fp.e)};
+        Wm2 = Wm1; Wm1 = W;
+        Um2 = Um1; Um1 = U;
+        Rp = R; Fp = F;
+        return N;
+    }
+};
 
 // Vector loads/stores of VEC consecutive elements (16 B, 8 B or scalar).
 template <class T, int V> __device__ __forceinline__ void ld_vec(const T* p, T (&o)[V]) {
@@ -206,30 +202,36 @@ __device__ __forceinline__ void warp_arrive(Ctl* ctl, T smax, bool bad, bool tim
 }
 
 // ---------------------------------------------------------------------------
-// x-sweep: Uold (S buffer) -> Utmp.  One warp per (row, x-segment).
-// src/cpu/solver_cpu.cpp:206-238 + :437-461
+// x-sweep: Uold (S buffer) -> Utmp.  One warp per (32-row group, x-segment),
+// one row per lane.  src/cpu/solver_cpu.cpp:206-238 + :437-461
 // ---------------------------------------------------------------------------
-template <class T, int S, int VEC, int STAGES, int NW>
-__global__ void __launch_bounds__(NW * 32)
+template <class T, int S, int STAGES, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB)
     sweep_x_kernel(const __grid_constant__ CUtensorMap tm, const SweepArgs<T> a) {
-    constexpr int W = 32 * VEC;
-    constexpr int STAGE = 4 * W;
+    constexpr int CX = 32 / sizeof(T);          // columns per box: 32-byte rows
+    constexpr int HV = CX / 2;                  // cells per 16-byte half row
+    constexpr int STAGE = 4 * 32 * CX;          // elements: 4 fields x 32 rows x CX
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
-    extern __shared__ __align__(128) unsigned char smem[];
+    static_assert(STAGE_BYTES % 1024 == 0, "32-byte swizzle needs 1 KB-aligned stage buffers");
+    extern __shared__ __align__(1024) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int task = blockIdx.x * NW + warp;
     if (task >= a.ntasks) return;
     Ctl* ctl = a.ctl;
     if (__ldcg(&ctl->done)) return;
 
-    T* buf = reinterpret_cast<T*>(smem) + (size_t)warp * STAGES * STAGE;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
+    // stage buffers on a 1 KB boundary (the launch reserves 1 KB of slack)
+    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+    T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
 
-    const int j = task / a.nseg;                 // interior row
-    const int s0 = (task - j * a.nseg) * a.seg;  // first interior column of this task
+    const int rg = task / a.nseg;                // 32-row group
+    const int s0 = (task - rg * a.nseg) * a.seg; // first interior column of the segment
     const int e = min(s0 + a.seg, a.nx);
-    const int nchunks = (e + 4 - s0 + W - 1) / W;
-    const double lam_d = __ldcg(&ctl->dt) / a.d;  // dt/dx
+    const int nst = (e + 4 - s0 + CX - 1) / CX;  // boxes: S columns [s0, e+4)
+    const int j = rg * 32 + lane;                // interior row of this lane
+    const bool row_ok = j < a.ny;
+    const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dx
     const T lam = T(lam_d);
     const T hl = T(0.5 * lam_d);
     const unsigned int req = __ldcg(&ctl->snap_req);
@@ -245,10 +247,10 @@ __global__ void __launch_bounds__(NW * 32)
         const int s = k % STAGES;
         const uint32_t b = smem_u32(&bar[s]);
         mbar_arrive_expect_tx(b, STAGE_BYTES);
-        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, s0 + k * W, j + 2, 0);
+        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, s0 + k * CX, rg * 32 + 2, 0);
     };
     if (lane == 0) {
-        const int np = min(STAGES, nchunks);
+        const int np = min(STAGES, nst);
         for (int k = 0; k < np; ++k) issue(k);
     }
 
@@ -258,106 +260,75 @@ __global__ void __launch_bounds__(NW * 32)
     int grow[4];
     bool gneg[4];
     int nghost = 0;
-    if (a.bc_lo == kBcReflective) {
-        if (j == 0) { grow[nghost] = 1; gneg[nghost++] = true; }
-        if (j == 1) { grow[nghost] = 0; gneg[nghost++] = true; }
-    } else if (j == 0) {
-        grow[nghost] = 1; gneg[nghost++] = false;
-        grow[nghost] = 0; gneg[nghost++] = false;
-    }
-    if (a.bc_hi == kBcReflective) {
-        if (j == a.ny - 1) { grow[nghost] = a.ny + 2; gneg[nghost++] = true; }
-        if (j == a.ny - 2) { grow[nghost] = a.ny + 3; gneg[nghost++] = true; }
-    } else if (j == a.ny - 1) {
-        grow[nghost] = a.ny + 2; gneg[nghost++] = false;
-        grow[nghost] = a.ny + 3; gneg[nghost++] = false;
+    if (row_ok) {
+        if (a.bc_lo == kBcReflective) {
+            if (j == 0) { grow[nghost] = 1; gneg[nghost++] = true; }
+            if (j == 1) { grow[nghost] = 0; gneg[nghost++] = true; }
+        } else if (j == 0) {
+            grow[nghost] = 1; gneg[nghost++] = false;
+            grow[nghost] = 0; gneg[nghost++] = false;
+        }
+        if (a.bc_hi == kBcReflective) {
+            if (j == a.ny - 1) { grow[nghost] = a.ny + 2; gneg[nghost++] = true; }
+            if (j == a.ny - 2) { grow[nghost] = a.ny + 3; gneg[nghost++] = true; }
+        } else if (j == a.ny - 1) {
+            grow[nghost] = a.ny + 2; gneg[nghost++] = false;
+            grow[nghost] = a.ny + 3; gneg[nghost++] = false;
+        }
     }
 
-    Prim<T> cW1{}, cW2{};
-    Cons<T> cU1{}, cU2{}, cF{};
-    Face<T> cR{};
+    Line<T, S> line;
+    line.reset();
+    const int swz = (lane >> 2) & 1;             // 32-byte swizzle: 16 B chunk ^= row bit 2
     bool timed_out = false;
-    int kfail = nchunks;
-    for (int k = 0; k < nchunks; ++k) {
+    int kfail = nst;
+    for (int k = 0; k < nst; ++k) {
         const int s = k % STAGES;
         if (!mbar_wait_bounded(smem_u32(&bar[s]), (uint32_t)((k / STAGES) & 1))) {
             timed_out = true;
             kfail = k;
             break;
         }
-        Cons<T> Ux[VEC + 2];
-        {
-            const T* sb = buf + s * STAGE + lane * VEC;
-            T r[VEC], mn[VEC], mt[VEC], en[VEC];
-            ld_vec<T, VEC>(sb, r);
-            ld_vec<T, VEC>(sb + W, mn);
-            ld_vec<T, VEC>(sb + 2 * W, mt);
-            ld_vec<T, VEC>(sb + 3 * W, en);
+        const T* rowp = buf + s * STAGE + lane * CX;
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) Ux[v + 2] = Cons<T>{r[v], mn[v], mt[v], en[v]};
-        }
-        __syncwarp();
-        if (lane == 0 && k + STAGES < nchunks) {
-            fence_proxy_async_smem();
-            issue(k + STAGES);
-        }
-        const int c0 = s0 + k * W + lane * VEC;  // S-buffer column of slot 0
-
-        if (snap) {  // the input state is a requested snapshot
+        for (int h = 0; h < 2; ++h) {
+            const T* q = rowp + ((h ^ swz) * HV);
+            T r[HV], mn[HV], mt[HV], en[HV];
+            ld_vec<T, HV>(q, r);
+            ld_vec<T, HV>(q + 32 * CX, mn);
+            ld_vec<T, HV>(q + 64 * CX, mt);
+            ld_vec<T, HV>(q + 96 * CX, en);
+            const int c0 = s0 + k * CX + h * HV;  // S column of the first cell of this half
+            Cons<T> N[HV];
+            unsigned mask = 0u;
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) {
-                const int ic = c0 + v - 2;
-                if (ic >= s0 && ic < e) {
-                    T* q = snap + (long long)j * a.nx + ic;
-                    q[0] = Ux[v + 2].r;
-                    q[a.snap_plane] = Ux[v + 2].mn;
-                    q[2 * a.snap_plane] = Ux[v + 2].mt;
-                    q[3 * a.snap_plane] = Ux[v + 2].e;
+            for (int v = 0; v < HV; ++v) {
+                const Cons<T> U{r[v], mn[v], mt[v], en[v]};
+                N[v] = line.push(U, hl, lam);
+                const int ic = c0 + v - 4;        // interior column of N[v]
+                if (ic >= s0 && ic < e) mask |= 1u << v;
+                if (snap && row_ok) {             // the input state is a requested snapshot
+                    const int is = c0 + v - 2;
+                    if (is >= s0 && is < e) {
+                        T* p = snap + (long long)j * a.nx + is;
+                        p[0] = U.r; p[a.snap_plane] = U.mn; p[2 * a.snap_plane] = U.mt; p[3 * a.snap_plane] = U.e;
+                    }
                 }
             }
+            if (mask && row_ok) {
+                store_cells<T, HV>(a.out, j + 2, c0, N, mask, 1, 2, false);
+                for (int g = 0; g < nghost; ++g) store_cells<T, HV>(a.out, grow[g], c0, N, mask, 1, 2, gneg[g]);
+            }
         }
-
-        // primitives of this box's cells; neighbours from the previous owner
-        Prim<T> Wx[VEC + 2];
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) Wx[v + 2] = cons_to_prim(Ux[v + 2]);
-        Wx[1] = prev_prim4(Wx[VEC + 1], cW1, lane);
-        Wx[0] = prev_prim4(Wx[VEC], cW2, lane);
-        Ux[1] = prev_of(Ux[VEC + 1], cU1, lane);
-        Ux[0] = prev_of(Ux[VEC], cU2, lane);
-
-        // slot v reconstructs cell c0+v-1, solves face (c0+v-2 | c0+v-1) and
-        // updates cell c0+v-2
-        Face<T> L[VEC], R[VEC];
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) reconstruct(Wx[v], Wx[v + 1], Wx[v + 2], hl, L[v], R[v]);
-        const Face<T> Rm = prev_face(R[VEC - 1], cR, lane);
-        Cons<T> F[VEC];
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) {
-            const Face<T>& left = (v == 0) ? Rm : R[v - 1];
-            F[v] = riemann<S>(left.U, left.V, L[v].U, L[v].V);
-        }
-        const Cons<T> Fm = prev_of(F[VEC - 1], cF, lane);
-        Cons<T> N[VEC];
-        unsigned mask = 0u;
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) {
-            const Cons<T>& fm = (v == 0) ? Fm : F[v - 1];
-            // src/cpu/solver_cpu.cpp:452-453
-            N[v] = Cons<T>{Ux[v].r - lam * (F[v].r - fm.r), Ux[v].mn - lam * (F[v].mn - fm.mn),
-                           Ux[v].mt - lam * (F[v].mt - fm.mt), Ux[v].e - lam * (F[v].e - fm.e)};
-            const int ic = c0 + v - 4;
-            if (ic >= s0 && ic < e) mask |= 1u << v;
-        }
-        if (mask) {
-            store_cells<T, VEC>(a.out, j + 2, c0, N, mask, 1, 2, false);
-            for (int q = 0; q < nghost; ++q) store_cells<T, VEC>(a.out, grow[q], c0, N, mask, 1, 2, gneg[q]);
+        __syncwarp();
+        if (lane == 0 && k + STAGES < nst) {
+            fence_proxy_async_smem();
+            issue(k + STAGES);
         }
     }
     if (timed_out) {
         // drain the boxes still in flight (bounded), then report
-        const int last = min(kfail + STAGES, nchunks);
+        const int last = min(kfail + STAGES, nst);
         for (int k = kfail + 1; k < last; ++k)
             (void)mbar_wait_bounded(smem_u32(&bar[k % STAGES]), (uint32_t)((k / STAGES) & 1));
         if (lane == 0) atomicOr(&ctl->status, (int)kStatusTimeout);
@@ -366,33 +337,34 @@ __global__ void __launch_bounds__(NW * 32)
 
 // ---------------------------------------------------------------------------
 // y-sweep: Utmp -> Unew (S buffer), with the fused CFL reduction.  One warp
-// per (row segment, column group).  src/cpu/solver_cpu.cpp:247-279 + :474-498
+// per (row segment, 32-column group), one column per lane.
+// src/cpu/solver_cpu.cpp:247-279 + :474-498
 // ---------------------------------------------------------------------------
-template <class T, int S, int VEC, int RY, int BW, int OFF, int STAGES, int NW>
-__global__ void __launch_bounds__(NW * 32)
+template <class T, int S, int RY, int STAGES, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB)
     sweep_y_kernel(const __grid_constant__ CUtensorMap tm, const SweepArgs<T> a) {
-    constexpr int WY = 32 * VEC;
-    constexpr int STAGE = 4 * RY * BW;
+    constexpr int STAGE = 4 * RY * 32;
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
-    static_assert(4 - OFF + WY <= BW, "box too narrow");
-    extern __shared__ __align__(128) unsigned char smem[];
+    static_assert(STAGE_BYTES % 128 == 0, "stage buffers must stay 128-byte aligned");
+    extern __shared__ __align__(1024) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int task = blockIdx.x * NW + warp;
     if (task >= a.ntasks) return;
     Ctl* ctl = a.ctl;
     if (__ldcg(&ctl->done)) return;
 
-    T* buf = reinterpret_cast<T*>(smem) + (size_t)warp * STAGES * STAGE;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
+    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+    T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
 
     const int rs = task / a.nseg;                // row segment
-    const int g = task - rs * a.nseg;            // column group
+    const int g = task - rs * a.nseg;            // 32-column group
     const int r0 = rs * a.seg;                   // first interior output row
     const int e = min(r0 + a.seg, a.ny);
-    const int nrows = e + 4 - r0;
-    const int nst = (nrows + RY - 1) / RY;
-    const int i0 = g * WY - OFF + lane * VEC;    // interior column of slot 0
-    const double lam_d = __ldcg(&ctl->dt) / a.d;
+    const int nst = (e + 4 - r0 + RY - 1) / RY;  // boxes: Utmp rows [r0, e+4)
+    const int i = g * 32 + lane;                 // interior column of this lane
+    const bool col_ok = i < a.nx;
+    const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dy
     const T lam = T(lam_d);
     const T hl = T(0.5 * lam_d);
 
@@ -406,26 +378,15 @@ __global__ void __launch_bounds__(NW * 32)
         const int s = k % STAGES;
         const uint32_t b = smem_u32(&bar[s]);
         mbar_arrive_expect_tx(b, STAGE_BYTES);
-        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, g * WY, r0 + k * RY, 0);
+        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, g * 32 + 4, r0 + k * RY, 0);
     };
     if (lane == 0) {
         const int np = min(STAGES, nst);
         for (int k = 0; k < np; ++k) issue(k);
     }
 
-    unsigned colmask = 0u;
-#pragma unroll
-    for (int v = 0; v < VEC; ++v)
-        if (i0 + v >= 0 && i0 + v < a.nx) colmask |= 1u << v;
-
-    Prim<T> Wm2[VEC], Wm1[VEC];
-    Cons<T> Um2[VEC], Um1[VEC], Fp[VEC];
-    Face<T> Rp[VEC];
-#pragma unroll
-    for (int v = 0; v < VEC; ++v) {
-        Wm2[v] = Prim<T>{}; Wm1[v] = Prim<T>{}; Um2[v] = Cons<T>{}; Um1[v] = Cons<T>{};
-        Fp[v] = Cons<T>{}; Rp[v] = Face<T>{};
-    }
+    Line<T, S> line;
+    line.reset();
     T smax = T(0);
     bool bad = false, timed_out = false;
     int kfail = nst;
@@ -436,66 +397,38 @@ __global__ void __launch_bounds__(NW * 32)
             kfail = k;
             break;
         }
-        Cons<T> U[RY][VEC];
+        const T* sb = buf + s * STAGE + lane;
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
-            const T* sb = buf + s * STAGE + rr * BW + (4 - OFF) + lane * VEC;
-            T r[VEC], mu[VEC], mv[VEC], en[VEC];
-            ld_vec<T, VEC>(sb, r);
-            ld_vec<T, VEC>(sb + RY * BW, mu);
-            ld_vec<T, VEC>(sb + 2 * RY * BW, mv);
-            ld_vec<T, VEC>(sb + 3 * RY * BW, en);
-#pragma unroll
-            for (int v = 0; v < VEC; ++v) U[rr][v] = Cons<T>{r[v], mv[v], mu[v], en[v]};  // n = y
+            // normal momentum of the y-sweep is rho*v (plane 2)
+            const Cons<T> U{sb[rr * 32], sb[(2 * RY + rr) * 32], sb[(RY + rr) * 32], sb[(3 * RY + rr) * 32]};
+            const Cons<T> N = line.push(U, hl, lam);
+            const int ir = r0 + k * RY + rr - 4;  // interior row of N
+            if (ir >= r0 && ir < e && col_ok) {
+                store_cell(a.out, ir + 2, i + 2, N, 2, 1, false);
+                const T sp = max_signal_speed(N);
+                bad |= !(sp < T(INFINITY));
+                smax = Ar<T>::fmax_(smax, sp);
+                // x-ghost columns of Unew read by the next x-sweep
+                if (i == 0) {
+                    if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, 1, N, 2, 1, true);
+                    else { store_cell(a.out, ir + 2, 1, N, 2, 1, false);
+                           store_cell(a.out, ir + 2, 0, N, 2, 1, false); }
+                }
+                if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, 0, N, 2, 1, true);
+                if (i == a.nx - 1) {
+                    if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + 2, N, 2, 1, true);
+                    else { store_cell(a.out, ir + 2, a.nx + 2, N, 2, 1, false);
+                           store_cell(a.out, ir + 2, a.nx + 3, N, 2, 1, false); }
+                }
+                if (i == a.nx - 2 && a.bc_hi == kBcReflective)
+                    store_cell(a.out, ir + 2, a.nx + 3, N, 2, 1, true);
+            }
         }
         __syncwarp();
         if (lane == 0 && k + STAGES < nst) {
             fence_proxy_async_smem();
             issue(k + STAGES);
-        }
-#pragma unroll
-        for (int rr = 0; rr < RY; ++rr) {
-            const int R = r0 + k * RY + rr;      // Utmp row of the freshest cells
-            Cons<T> N[VEC];
-#pragma unroll
-            for (int v = 0; v < VEC; ++v) {
-                const Prim<T> W = cons_to_prim(U[rr][v]);
-                Face<T> L, Rn;
-                reconstruct(Wm2[v], Wm1[v], W, hl, L, Rn);           // cell row R-1
-                const Cons<T> F = riemann<S>(Rp[v].U, Rp[v].V, L.U, L.V);  // face (R-2 | R-1)
-                // src/cpu/solver_cpu.cpp:489-490, cell row R-2
-                N[v] = Cons<T>{Um2[v].r - lam * (F.r - Fp[v].r), Um2[v].mn - lam * (F.mn - Fp[v].mn),
-                               Um2[v].mt - lam * (F.mt - Fp[v].mt), Um2[v].e - lam * (F.e - Fp[v].e)};
-                Wm2[v] = Wm1[v]; Wm1[v] = W;
-                Um2[v] = Um1[v]; Um1[v] = U[rr][v];
-                Rp[v] = Rn; Fp[v] = F;
-            }
-            const int ir = R - 4;                // interior row of N
-            if (ir >= r0 && ir < e && colmask) {
-                store_cells<T, VEC>(a.out, ir + 2, i0 + 2, N, colmask, 2, 1, false);
-#pragma unroll
-                for (int v = 0; v < VEC; ++v) {
-                    if (!(colmask & (1u << v))) continue;
-                    const T sp = max_signal_speed(N[v]);
-                    bad |= !(sp < T(INFINITY));
-                    smax = Ar<T>::fmax_(smax, sp);
-                    // x-ghost columns of Unew read by the next x-sweep
-                    const int ic = i0 + v;
-                    if (ic == 0) {
-                        if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, 1, N[v], 2, 1, true);
-                        else { store_cell(a.out, ir + 2, 1, N[v], 2, 1, false);
-                               store_cell(a.out, ir + 2, 0, N[v], 2, 1, false); }
-                    }
-                    if (ic == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, 0, N[v], 2, 1, true);
-                    if (ic == a.nx - 1) {
-                        if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + 2, N[v], 2, 1, true);
-                        else { store_cell(a.out, ir + 2, a.nx + 2, N[v], 2, 1, false);
-                               store_cell(a.out, ir + 2, a.nx + 3, N[v], 2, 1, false); }
-                    }
-                    if (ic == a.nx - 2 && a.bc_hi == kBcReflective)
-                        store_cell(a.out, ir + 2, a.nx + 3, N[v], 2, 1, true);
-                }
-            }
         }
     }
     if (timed_out) {

@@ -93,6 +93,7 @@ struct eu_handle {
     int cur = 0;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 0;
+    int l2promo_x = 256, l2promo_y = 256;   // TMA L2 promotion (bytes) of the sweep inputs
     std::string err;
 };
 
@@ -122,8 +123,17 @@ template <class T> Planes<T> planes_t(const eu_handle* h) {
     return Planes<T>{static_cast<T*>(h->Tm), h->pitch_t, h->plane_t};
 }
 
+CUtensorMapL2promotion promo_of(int bytes) {
+    switch (bytes) {
+        case 0: return CU_TENSOR_MAP_L2_PROMOTION_NONE;
+        case 64: return CU_TENSOR_MAP_L2_PROMOTION_L2_64B;
+        case 128: return CU_TENSOR_MAP_L2_PROMOTION_L2_128B;
+        default: return CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
+    }
+}
+
 int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long pitch, long long plane,
-           int box_w, int box_h, CUtensorMapSwizzle swz) {
+           int box_w, int box_h, CUtensorMapSwizzle swz, int promo) {
     auto fn = encode_fn();
     if (!fn) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
     const cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)(h->cfg.ny + 4), 4};
@@ -132,10 +142,19 @@ int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long 
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = fn(m, h->prec == EU_FP32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
                           3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          swz, promo_of(promo),
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return EU_OK;
+}
+
+int encode_all(eu_handle* h) {
+    for (int b = 0; b < 2; ++b)
+        if (int rc = encode(h, &h->tm_x[b], h->S[b], h->cfg.nx + 4, h->pitch_s, h->plane_s, h->K.box_x, 32,
+                            CU_TENSOR_MAP_SWIZZLE_32B, h->l2promo_x))
+            return rc;
+    return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  h->l2promo_y);
 }
 
 // Work decomposition: enough independent warps to fill every SM a few times
@@ -448,13 +467,7 @@ int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limite
     if (e != cudaSuccess) { g_err = std::string("allocation: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
     ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
     if (ctl_push(h)) { g_err = h->err; return bail(EU_ERR_CUDA); }
-    for (int b = 0; b < 2; ++b)
-        if (encode(h, &h->tm_x[b], h->S[b], cfg->nx + 4, h->pitch_s, h->plane_s, h->K.box_x, 32,
-                   CU_TENSOR_MAP_SWIZZLE_32B)) {
-            g_err = h->err;
-            return bail(EU_ERR_CUDA);
-        }
-    if (encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE)) {
+    if (encode_all(h)) {
         g_err = h->err;
         return bail(EU_ERR_CUDA);
     }
@@ -857,6 +870,49 @@ int eu_get_dt_log(eu_handle* h, double* out, long long n) {
     if (n == 0) return EU_OK;
     EU_CUDA(h, cudaMemcpyAsync(out, h->d_dtlog, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->st));
     EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_set_option(eu_handle* h, const char* name, long long value) {
+    if (!h || !name) return fail(h, EU_ERR_INVALID, "null argument");
+    const std::string k(name);
+    if (k == "l2_promotion_x" || k == "l2_promotion_y") {
+        if (value != 0 && value != 64 && value != 128 && value != 256)
+            return fail(h, EU_ERR_INVALID, "L2 promotion must be 0, 64, 128 or 256 bytes");
+        (k == "l2_promotion_x" ? h->l2promo_x : h->l2promo_y) = (int)value;
+        if (int rc = encode_all(h)) return rc;
+    } else if (k == "seg_x") {
+        if (value < h->K.box_x || value % h->K.box_x) return fail(h, EU_ERR_INVALID, "seg_x must be a multiple of the box width");
+        h->seg_x = (int)value;
+        h->nseg_x = (h->cfg.nx + h->seg_x - 1) / h->seg_x;
+        h->ntasks_x = ((h->cfg.ny + 31) / 32) * h->nseg_x;
+        h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
+    } else if (k == "seg_y") {
+        if (value < 1) return fail(h, EU_ERR_INVALID, "seg_y must be >= 1");
+        h->seg_y = (int)value;
+        h->ntasks_y = h->nseg_y * ((h->cfg.ny + h->seg_y - 1) / h->seg_y);
+        h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
+    } else if (k == "graph_steps") {
+        if (value < 1 || value > 4096) return fail(h, EU_ERR_INVALID, "graph_steps must be in [1, 4096]");
+        h->gsteps = (int)value;
+    } else {
+        return fail(h, EU_ERR_INVALID, "unknown option " + k);
+    }
+    drop_graphs(h);
+    return EU_OK;
+}
+
+int eu_get_option(eu_handle* h, const char* name, long long* value) {
+    if (!h || !name || !value) return fail(h, EU_ERR_INVALID, "null argument");
+    const std::string k(name);
+    if (k == "l2_promotion_x") *value = h->l2promo_x;
+    else if (k == "l2_promotion_y") *value = h->l2promo_y;
+    else if (k == "seg_x") *value = h->seg_x;
+    else if (k == "seg_y") *value = h->seg_y;
+    else if (k == "graph_steps") *value = h->gsteps;
+    else if (k == "tasks_x") *value = h->ntasks_x;
+    else if (k == "tasks_y") *value = h->ntasks_y;
+    else return fail(h, EU_ERR_INVALID, "unknown option " + k);
     return EU_OK;
 }
 

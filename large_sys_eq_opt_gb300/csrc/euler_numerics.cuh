@@ -417,6 +417,172 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
     R.V = okR ? Vcr : VUR;
 }
 
+// ---------------------------------------------------------------------------
+// Fast path.  The common case of every branch above, computed straight-line;
+// `slow` is set whenever any of the reference's fallback branches (or the
+// FP64 pressure island) could change the result.  A lane with `slow` set
+// recomputes the cell with the full functions above, so results equal the
+// full path bit for bit while the hot loop carries no fallback code.
+// ---------------------------------------------------------------------------
+// All four finite (NaN and inf propagate through the sum; a sum that only
+// overflows needs |values| ~ 1e38 / 1e308 and is treated as non-finite).
+template <class T> __device__ __forceinline__ bool finite4(T a, T b, T c, T d) {
+    return Ar<T>::fabs_((a + b) + (c + d)) < T(INFINITY);
+}
+// physical_recon, with the 1e-12 floors (src/cpu/solver_cpu.cpp:39-43)
+template <class T> __device__ __forceinline__ bool phys_recon_fast(const Prim<T>& V) {
+    return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(kRhoFloorD);
+}
+// physical_riemann (head/riemann.hpp:74-81)
+template <class T> __device__ __forceinline__ bool phys_riemann_fast(const Prim<T>& V) {
+    return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(0);
+}
+
+// cons_to_prim without the FP64 island; flags the states that need it.
+template <class T> __device__ __forceinline__ Prim<T> c2p_fast(const Cons<T>& U, bool& slow) {
+    if constexpr (sizeof(T) == 8) {
+        return cons_to_prim(U);
+    } else {
+        Prim<T> V;
+        V.ir = Ar<T>::rcp(U.r);
+        V.r = U.r;
+        V.un = U.mn * V.ir;
+        V.ut = U.mt * V.ir;
+        const T kinetic = T(0.5) * U.r * (V.un * V.un + V.ut * V.ut);
+        V.p = gm1<T>() * (U.e - kinetic);
+        slow |= T(2) * kinetic > U.e;
+        return V;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void reconstruct_fast(const Prim<T>& Wm, const Prim<T>& Wc, const Prim<T>& Wp,
+                                                 T hl, Face<T>& L, Face<T>& R, bool& slow) {
+    Prim<T> s;
+    s.r = minmod(Wc.r - Wm.r, Wp.r - Wc.r);
+    s.un = minmod(Wc.un - Wm.un, Wp.un - Wc.un);
+    s.ut = minmod(Wc.ut - Wm.ut, Wp.ut - Wc.ut);
+    s.p = minmod(Wc.p - Wm.p, Wp.p - Wc.p);
+    const Prim<T> WL{Wc.r - T(0.5) * s.r, Wc.un - T(0.5) * s.un, Wc.ut - T(0.5) * s.ut, Wc.p - T(0.5) * s.p, T(0)};
+    const Prim<T> WR{Wc.r + T(0.5) * s.r, Wc.un + T(0.5) * s.un, Wc.ut + T(0.5) * s.ut, Wc.p + T(0.5) * s.p, T(0)};
+    const bool okW = phys_recon_fast(WL) && phys_recon_fast(WR);
+    const Cons<T> UL = prim_to_cons(WL), UR = prim_to_cons(WR);
+    Cons<T> FL, FR;
+    if constexpr (sizeof(T) == 8) {
+        FL = flux(UL, cons_to_prim(UL));
+        FR = flux(UR, cons_to_prim(UR));
+    } else {
+        FL = flux(UL, WL);
+        FR = flux(UR, WR);
+    }
+    const Cons<T> h{hl * (FR.r - FL.r), hl * (FR.mn - FL.mn), hl * (FR.mt - FL.mt), hl * (FR.e - FL.e)};
+    L.U = Cons<T>{UL.r - h.r, UL.mn - h.mn, UL.mt - h.mt, UL.e - h.e};
+    R.U = Cons<T>{UR.r - h.r, UR.mn - h.mn, UR.mt - h.mt, UR.e - h.e};
+    L.V = c2p_fast(L.U, slow);
+    R.V = c2p_fast(R.U, slow);
+    slow |= !(okW && phys_recon_fast(L.V) && phys_recon_fast(R.V));
+}
+
+// Riemann fluxes for physical inputs (the face states of reconstruct_fast).
+template <class T>
+__device__ __forceinline__ Cons<T> hll_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
+                                            const Prim<T>& VR, bool& slow) {
+    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    const T aL = sound_speed(VL), aR = sound_speed(VR);
+    const T SL = Ar<T>::fmin_(VL.un - aL, VR.un - aR);
+    const T SR = Ar<T>::fmax_(VL.un + aL, VR.un + aR);
+    const T den = SR - SL;
+    const T id = Ar<T>::rcp(den), ss = SL * SR;
+    const Cons<T> Fh{(SR * FL.r - SL * FR.r + ss * (UR.r - UL.r)) * id,
+                     (SR * FL.mn - SL * FR.mn + ss * (UR.mn - UL.mn)) * id,
+                     (SR * FL.mt - SL * FR.mt + ss * (UR.mt - UL.mt)) * id,
+                     (SR * FL.e - SL * FR.e + ss * (UR.e - UL.e)) * id};
+    const bool upL = SL >= T(0), upR = SR <= T(0);
+    slow |= !(upL || upR || !(Ar<T>::fabs_(den) < T(1.0e-14)));
+    return upL ? FL : (upR ? FR : Fh);
+}
+
+template <class T>
+__device__ __forceinline__ Cons<T> hllc_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
+                                             const Prim<T>& VR, bool& slow) {
+    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    const T aL = sound_speed(VL), aR = sound_speed(VR);
+    const T unL = VL.un, unR = VR.un;
+    const T SL = Ar<T>::fmin_(unL - aL, unR - aR);
+    const T SR = Ar<T>::fmax_(unL + aL, unR + aR);
+    const T qL = VL.r * (SL - unL), qR = VR.r * (SR - unR);
+    const T numerator = VR.p - VL.p + qL * unL - qR * unR;
+    const T denominator = qL - qR;
+    const T Sstar = numerator * Ar<T>::rcp(denominator);
+    const bool left = Sstar >= T(0);
+    const Cons<T> U = left ? UL : UR;
+    const Cons<T> F = left ? FL : FR;
+    const T rho = left ? VL.r : VR.r;
+    const T p = left ? VL.p : VR.p;
+    const T un = left ? unL : unR;
+    const T ut = left ? VL.ut : VR.ut;
+    const T irho = left ? VL.ir : VR.ir;
+    const T S = left ? SL : SR;
+    const T dS = S - Sstar;
+    const T q = rho * (S - un);
+    const T rho_star = q * Ar<T>::rcp(dS);
+    const T E_star = rho_star * (U.e * irho + (Sstar - un) * (Sstar + p * Ar<T>::rcp(q)));
+    const Cons<T> Fs{F.r + S * (rho_star - U.r), F.mn + S * (rho_star * Sstar - U.mn),
+                     F.mt + S * (rho_star * ut - U.mt), F.e + S * (E_star - U.e)};
+    const bool upL = SL >= T(0), upR = SR <= T(0);
+    const bool ok = !(Ar<T>::fabs_(denominator) < T(1.0e-14)) && !(Ar<T>::fabs_(dS) < T(1.0e-14)) &&
+                    Ar<T>::fabs_(Sstar + rho_star + E_star) < T(INFINITY) && rho_star > T(0);
+    slow |= !(upL || upR || ok);
+    return upL ? FL : (upR ? FR : Fs);
+}
+
+template <class T>
+__device__ __forceinline__ Cons<T> force_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
+                                              const Prim<T>& VR, bool& slow) {
+    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    const Cons<T> Fc = c_avg(FL, FR);
+    const T aL = sound_speed(VL), aR = sound_speed(VR);
+    const T alpha = Ar<T>::fmax_(Ar<T>::fabs_(VL.un) + aL, Ar<T>::fabs_(VR.un) + aR);
+    const T ha = T(0.5) * alpha;
+    const T hia = T(0.5) * Ar<T>::rcp(alpha);
+    const Cons<T> Flf{Fc.r - ha * (UR.r - UL.r), Fc.mn - ha * (UR.mn - UL.mn),
+                      Fc.mt - ha * (UR.mt - UL.mt), Fc.e - ha * (UR.e - UL.e)};
+    const Cons<T> Ua = c_avg(UL, UR);
+    const Cons<T> Uri{Ua.r - hia * (FR.r - FL.r), Ua.mn - hia * (FR.mn - FL.mn),
+                      Ua.mt - hia * (FR.mt - FL.mt), Ua.e - hia * (FR.e - FL.e)};
+    const Prim<T> Vri = c2p_fast(Uri, slow);
+    slow |= !(Ar<T>::finite(alpha) && alpha > T(1.0e-14) && phys_riemann_fast(Vri));
+    return c_avg(Flf, flux(Uri, Vri));
+}
+
+template <int S, class T>
+__device__ __forceinline__ Cons<T> riemann_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
+                                                const Prim<T>& VR, bool& slow) {
+    if constexpr (S == kHLLC) return hllc_fast(UL, VL, UR, VR, slow);
+    else if constexpr (S == kFORCE) return force_fast(UL, VL, UR, VR, slow);
+    else if constexpr (S == kHLL) return hll_fast(UL, VL, UR, VR, slow);
+    else return exact_flux(UL, VL, UR, VR);   // the exact solver always takes its full path
+}
+
+// Full-logic recomputation of one cell (out of line; taken only by lanes
+// whose fast path flagged a fallback).
+template <class T> struct CellOut {
+    Prim<T> W;
+    Face<T> L, R;
+    Cons<T> F;
+    bool r_phys;   // R.V is physical (the next cell's fast Riemann needs it)
+};
+
+template <class T, int S>
+__device__ __noinline__ CellOut<T> cell_full(Cons<T> U, Prim<T> Wm2, Prim<T> Wm1, Face<T> Rp, T hl) {
+    CellOut<T> o;
+    o.W = cons_to_prim(U);
+    reconstruct(Wm2, Wm1, o.W, hl, o.L, o.R);
+    o.F = riemann<S>(Rp.U, Rp.V, o.L.U, o.L.V);
+    o.r_phys = physical_riemann(o.R.V);
+    return o;
+}
+
 // Largest signal speed max(|un|+a, |ut|+a) of a conserved state
 // (src/cpu/solver_cpu.cpp:295-300); NaN for a non-finite state.
 template <class T> __device__ __forceinline__ T max_signal_speed(const Cons<T>& U) {

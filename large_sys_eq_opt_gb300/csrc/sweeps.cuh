@@ -41,26 +41,35 @@ template <class T, int S> struct Line {
     Cons<T> Um2, Um1;   // conserved states of cells c-2, c-1
     Face<T> Rp;         // evolved right face state of cell c-2
     Cons<T> Fp;         // flux through face (c-3 | c-2)
+    bool rp_phys;       // Rp is physical (always true when it came from the fast path)
 
     __device__ __forceinline__ void reset() {
         Wm2 = Prim<T>{}; Wm1 = Prim<T>{}; Um2 = Cons<T>{}; Um1 = Cons<T>{};
         Rp = Face<T>{}; Fp = Cons<T>{};
+        rp_phys = false;
     }
 
     __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
-        const Prim<T> W = cons_to_prim(U);
+        bool slow = !rp_phys;
+        Prim<T> W = c2p_fast(U, slow);
         Face<T> L, R;
-        reconstruct(Wm2, Wm1, W, hl, L, R);
-        const Cons<T> F = riemann<S>(Rp.U, Rp.V, L.U, L.V);
+        reconstruct_fast(Wm2, Wm1, W, hl, L, R, slow);
+        Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);
+        bool r_phys = true;
+        if (__builtin_expect(slow, 0)) {
+            const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl);
+            W = o.W; L = o.L; R = o.R; F = o.F;
+            r_phys = o.r_phys;
+        }
         const Cons<T> N{Um2.r - lam * (F.r - Fp.r), Um2.mn - lam * (F.mn - Fp.mn),
                         Um2.mt - lam * (F.mt - Fp.mt), Um2.e - lam * (F.e - Fp.e)};
         Wm2 = Wm1; Wm1 = W;
         Um2 = Um1; Um1 = U;
         Rp = R; Fp = F;
+        rp_phys = r_phys;
         return N;
     }
 };
-
 // Vector loads/stores of VEC consecutive elements (16 B, 8 B or scalar).
 template <class T, int V> __device__ __forceinline__ void ld_vec(const T* p, T (&o)[V]) {
     if constexpr (V == 1) {

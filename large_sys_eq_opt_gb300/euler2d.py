@@ -52,7 +52,7 @@ EXPORTS = (
     "eu_download_aos", "eu_compute_dt", "eu_advance", "eu_step_n", "eu_run", "eu_get_time",
     "eu_totals", "eu_compute_dt_host", "eu_advance_host", "eu_step_host", "eu_time_steps",
     "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
-    "eu_get_dt_log", "eu_set_device",
+    "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option",
 )
 
 _lib = None
@@ -105,6 +105,8 @@ def load(path: str = LIB_PATH):
     L.eu_set_dt_log.argtypes = [H, C.c_longlong]
     L.eu_get_dt_log.argtypes = [H, _dp, C.c_longlong]
     L.eu_set_device.argtypes = [C.c_int]
+    L.eu_set_option.argtypes = [H, C.c_char_p, C.c_longlong]
+    L.eu_get_option.argtypes = [H, C.c_char_p, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -241,6 +243,14 @@ class Solver:
         out = np.zeros(int(n))
         self._check(self._L.eu_get_dt_log(self._h, _p(out), int(n)))
         return out
+
+    def set_option(self, name: str, value: int):
+        self._check(self._L.eu_set_option(self._h, name.encode(), int(value)))
+
+    def get_option(self, name: str) -> int:
+        v = C.c_longlong()
+        self._check(self._L.eu_get_option(self._h, name.encode(), C.byref(v)))
+        return v.value
 
     def totals(self) -> np.ndarray:
         out = np.zeros(4)

@@ -87,6 +87,7 @@ struct eu_handle {
     long long dtlog_cap = 0;
     CUtensorMap tm_x[2];
     CUtensorMap tm_y;
+    CUtensorMap tm_xo;   // x-sweep output: Utmp boxes, rows [0, ny+2), columns [0, nx+4)
     SweepKernels K{};
     int seg_x = 0, nseg_x = 0, ntasks_x = 0, ctas_x = 0;
     int seg_y = 0, nseg_y = 0, ntasks_y = 0, ctas_y = 0;
@@ -133,10 +134,10 @@ CUtensorMapL2promotion promo_of(int bytes) {
 }
 
 int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long pitch, long long plane,
-           int box_w, int box_h, CUtensorMapSwizzle swz, int promo) {
+           int box_w, int box_h, CUtensorMapSwizzle swz, int promo, long long height = -1) {
     auto fn = encode_fn();
     if (!fn) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
-    const cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)(h->cfg.ny + 4), 4};
+    const cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)(height > 0 ? height : h->cfg.ny + 4), 4};
     const cuuint64_t strides[2] = {(cuuint64_t)(pitch * h->esz), (cuuint64_t)(plane * h->esz)};
     const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 4};
     const cuuint32_t estr[3] = {1, 1, 1};
@@ -153,6 +154,11 @@ int encode_all(eu_handle* h) {
         if (int rc = encode(h, &h->tm_x[b], h->S[b], h->cfg.nx + 4, h->pitch_s, h->plane_s, h->K.box_x, 32,
                             CU_TENSOR_MAP_SWIZZLE_32B, h->l2promo_x))
             return rc;
+    // x-sweep stores: width nx+4 and height ny+2 clip everything past the
+    // last interior column / row, so no box spills into the top ghost rows.
+    if (int rc = encode(h, &h->tm_xo, h->Tm, h->cfg.nx + 4, h->pitch_t, h->plane_t, h->K.box_x, 32,
+                        CU_TENSOR_MAP_SWIZZLE_32B, 256, h->cfg.ny + 2))
+        return rc;
     return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE,
                   h->l2promo_y);
 }
@@ -225,19 +231,19 @@ template <class T> SweepArgs<T> y_args(const eu_handle* h, int cur) {
 cudaError_t launch_x(eu_handle* h, int cur) {
     if (h->prec == EU_FP32) {
         const SweepArgs<float> a = x_args<float>(h, cur);
-        return h->K.x(&h->tm_x[cur], &a, h->ctas_x, h->st);
+        return h->K.x(&h->tm_x[cur], &h->tm_xo, &a, h->ctas_x, h->st);
     }
     const SweepArgs<double> a = x_args<double>(h, cur);
-    return h->K.x(&h->tm_x[cur], &a, h->ctas_x, h->st);
+    return h->K.x(&h->tm_x[cur], &h->tm_xo, &a, h->ctas_x, h->st);
 }
 
 cudaError_t launch_y(eu_handle* h, int cur) {
     if (h->prec == EU_FP32) {
         const SweepArgs<float> a = y_args<float>(h, cur);
-        return h->K.y(&h->tm_y, &a, h->ctas_y, h->st);
+        return h->K.y(&h->tm_y, nullptr, &a, h->ctas_y, h->st);
     }
     const SweepArgs<double> a = y_args<double>(h, cur);
-    return h->K.y(&h->tm_y, &a, h->ctas_y, h->st);
+    return h->K.y(&h->tm_y, nullptr, &a, h->ctas_y, h->st);
 }
 
 cudaError_t launch_step(eu_handle* h, int cur) {

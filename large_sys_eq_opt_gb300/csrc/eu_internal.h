@@ -72,8 +72,8 @@ template <class T> struct SweepArgs {
 };
 
 // Host-side launch entry of one sweep instantiation.
-using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const void* args, int ctas,
-                                    cudaStream_t s);
+using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args,
+                                    int ctas, cudaStream_t s);
 
 struct SweepKernels {
     SweepLaunch x, y;

@@ -22,7 +22,10 @@ namespace {
 
 #if EU_PREC == 32
 using T = float;
-constexpr int MINB_X = 4, MINB_Y = 4;   // 16 resident warps per SM (<= 128 registers)
+#ifndef EU_MINB_X
+#define EU_MINB_X 4
+#endif
+constexpr int MINB_X = EU_MINB_X, MINB_Y = 4;   // x: EU_MINB_X CTAs of 4 warps per SM; y: 16 warps (<= 128 registers)
 #else
 using T = double;
 constexpr int MINB_X = 2, MINB_Y = 2;
@@ -39,15 +42,17 @@ constexpr size_t kStageY = 4 * RY * 32 * sizeof(T);
 constexpr size_t kSmemX = 1024 + NW * SX * kStageX + NW * SX * sizeof(uint64_t);
 constexpr size_t kSmemY = 1024 + NW * SY * kStageY + NW * SY * sizeof(uint64_t);
 
-static cudaError_t LAUNCH_X(const CUtensorMap* tm, const void* args, int ctas, cudaStream_t s) {
+static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args, int ctas,
+                            cudaStream_t s) {
     auto k = sweep_x_kernel<T, SOL, SX, NW, MINB_X>;
     static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX);
     if (attr != cudaSuccess) return attr;
-    k<<<ctas, NW * 32, kSmemX, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
+    k<<<ctas, NW * 32, kSmemX, s>>>(*tm, *tm_out, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
 }
 
-static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const void* args, int ctas, cudaStream_t s) {
+static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap*, const void* args, int ctas,
+                            cudaStream_t s) {
     auto k = sweep_y_kernel<T, SOL, RY, SY, NW, MINB_Y>;
     static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
     if (attr != cudaSuccess) return attr;

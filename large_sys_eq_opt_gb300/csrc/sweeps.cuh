@@ -213,10 +213,18 @@ __device__ __forceinline__ void warp_arrive(Ctl* ctl, T smax, bool bad, bool tim
 // ---------------------------------------------------------------------------
 // x-sweep: Uold (S buffer) -> Utmp.  One warp per (32-row group, x-segment),
 // one row per lane.  src/cpu/solver_cpu.cpp:206-238 + :437-461
+//
+// Box k holds S columns [m0 + 8k, m0 + 8k + 8) of 32 rows (m0 = s0 - 4 in
+// FP32 units of 32 bytes).  The cell updated when S column c is pushed is
+// interior column c - 4, which sits in Utmp column c: every output lands in
+// the shared-memory slot its input came from, so the box is overwritten in
+// place and written back with one TMA store.  Box 0 only warms the stencil
+// window up; boxes 1..seg/CX hold exactly this segment's outputs.
 // ---------------------------------------------------------------------------
 template <class T, int S, int STAGES, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB)
-    sweep_x_kernel(const __grid_constant__ CUtensorMap tm, const SweepArgs<T> a) {
+    sweep_x_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tm_out,
+                   const SweepArgs<T> a) {
     constexpr int CX = 32 / sizeof(T);          // columns per box: 32-byte rows
     constexpr int HV = CX / 2;                  // cells per 16-byte half row
     constexpr int STAGE = 4 * 32 * CX;          // elements: 4 fields x 32 rows x CX
@@ -237,7 +245,8 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     const int rg = task / a.nseg;                // 32-row group
     const int s0 = (task - rg * a.nseg) * a.seg; // first interior column of the segment
     const int e = min(s0 + a.seg, a.nx);
-    const int nst = (e + 4 - s0 + CX - 1) / CX;  // boxes: S columns [s0, e+4)
+    const int m0 = s0 - HV;                      // first S column marched (4 FP32 / 2 FP64 cells early)
+    const int nst = 1 + (e - s0 + CX - 1) / CX;  // warm-up box + output boxes
     const int j = rg * 32 + lane;                // interior row of this lane
     const bool row_ok = j < a.ny;
     const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dx
@@ -250,13 +259,14 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bar[s]), 1);
         fence_mbar_init();
         tma_prefetch_desc(&tm);
+        tma_prefetch_desc(&tm_out);
     }
     __syncwarp();
     auto issue = [&](int k) {
         const int s = k % STAGES;
         const uint32_t b = smem_u32(&bar[s]);
         mbar_arrive_expect_tx(b, STAGE_BYTES);
-        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, s0 + k * CX, rg * 32 + 2, 0);
+        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, m0 + k * CX, rg * 32 + 2, 0);
     };
     if (lane == 0) {
         const int np = min(STAGES, nst);
@@ -265,26 +275,24 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 
     // Ghost rows of Utmp fed by this row (the y-ghosts the y-sweep reads):
     // transmissive sides copy the edge row into both layers, reflective
-    // sides mirror rows 0/1 (ny-1/ny-2) with rho*v negated.
-    int grow[4];
-    bool gneg[4];
-    int nghost = 0;
+    // sides mirror rows 0/1 (ny-1/ny-2) with rho*v negated.  At most four.
+    int g0 = -1, g1 = -1, g2 = -1, g3 = -1;
+    bool n0 = false, n1 = false, n2 = false, n3 = false;
     if (row_ok) {
         if (a.bc_lo == kBcReflective) {
-            if (j == 0) { grow[nghost] = 1; gneg[nghost++] = true; }
-            if (j == 1) { grow[nghost] = 0; gneg[nghost++] = true; }
+            if (j == 0) { g0 = 1; n0 = true; }
+            if (j == 1) { g0 = 0; n0 = true; }
         } else if (j == 0) {
-            grow[nghost] = 1; gneg[nghost++] = false;
-            grow[nghost] = 0; gneg[nghost++] = false;
+            g0 = 1; g1 = 0;
         }
         if (a.bc_hi == kBcReflective) {
-            if (j == a.ny - 1) { grow[nghost] = a.ny + 2; gneg[nghost++] = true; }
-            if (j == a.ny - 2) { grow[nghost] = a.ny + 3; gneg[nghost++] = true; }
+            if (j == a.ny - 1) { g2 = a.ny + 2; n2 = true; }
+            if (j == a.ny - 2) { g2 = a.ny + 3; n2 = true; }
         } else if (j == a.ny - 1) {
-            grow[nghost] = a.ny + 2; gneg[nghost++] = false;
-            grow[nghost] = a.ny + 3; gneg[nghost++] = false;
+            g2 = a.ny + 2; g3 = a.ny + 3;
         }
     }
+    const bool has_ghost = g0 >= 0 || g2 >= 0;
 
     Line<T, S> line;
     line.reset();
@@ -298,24 +306,19 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             kfail = k;
             break;
         }
-        const T* rowp = buf + s * STAGE + lane * CX;
-#pragma unroll
+        T* rowp = buf + s * STAGE + lane * CX;
+#pragma unroll 1
         for (int h = 0; h < 2; ++h) {
-            const T* q = rowp + ((h ^ swz) * HV);
+            T* q = rowp + ((h ^ swz) * HV);
             T r[HV], mn[HV], mt[HV], en[HV];
             ld_vec<T, HV>(q, r);
             ld_vec<T, HV>(q + 32 * CX, mn);
             ld_vec<T, HV>(q + 64 * CX, mt);
             ld_vec<T, HV>(q + 96 * CX, en);
-            const int c0 = s0 + k * CX + h * HV;  // S column of the first cell of this half
-            Cons<T> N[HV];
-            unsigned mask = 0u;
+            const int c0 = m0 + k * CX + h * HV;  // S (and Utmp) column of the first cell
 #pragma unroll
             for (int v = 0; v < HV; ++v) {
                 const Cons<T> U{r[v], mn[v], mt[v], en[v]};
-                N[v] = line.push(U, hl, lam);
-                const int ic = c0 + v - 4;        // interior column of N[v]
-                if (ic >= s0 && ic < e) mask |= 1u << v;
                 if (snap && row_ok) {             // the input state is a requested snapshot
                     const int is = c0 + v - 2;
                     if (is >= s0 && is < e) {
@@ -323,18 +326,38 @@ __global__ void __launch_bounds__(NW * 32, MINB)
                         p[0] = U.r; p[a.snap_plane] = U.mn; p[2 * a.snap_plane] = U.mt; p[3 * a.snap_plane] = U.e;
                     }
                 }
+                const Cons<T> N = line.push(U, hl, lam);
+                r[v] = N.r; mn[v] = N.mn; mt[v] = N.mt; en[v] = N.e;
+                if (has_ghost && k > 0) {
+                    const int ic = c0 + v - 4;
+                    if (ic >= s0 && ic < e) {
+                        if (g0 >= 0) store_cell(a.out, g0, c0 + v, N, 1, 2, n0);
+                        if (g1 >= 0) store_cell(a.out, g1, c0 + v, N, 1, 2, n1);
+                        if (g2 >= 0) store_cell(a.out, g2, c0 + v, N, 1, 2, n2);
+                        if (g3 >= 0) store_cell(a.out, g3, c0 + v, N, 1, 2, n3);
+                    }
+                }
             }
-            if (mask && row_ok) {
-                store_cells<T, HV>(a.out, j + 2, c0, N, mask, 1, 2, false);
-                for (int g = 0; g < nghost; ++g) store_cells<T, HV>(a.out, grow[g], c0, N, mask, 1, 2, gneg[g]);
+            st_vec<T, HV>(q, r);                  // outputs overwrite their inputs in place
+            st_vec<T, HV>(q + 32 * CX, mn);
+            st_vec<T, HV>(q + 64 * CX, mt);
+            st_vec<T, HV>(q + 96 * CX, en);
+        }
+        fence_proxy_async_smem();                 // make the in-place writes visible to TMA
+        __syncwarp();
+        if (lane == 0) {
+            if (k > 0) {
+                tma_store_3d(&tm_out, smem_u32(buf + s * STAGE), m0 + k * CX, rg * 32 + 2, 0);
+                bulk_commit();
+            }
+            if (k + STAGES < nst) {
+                bulk_wait_read0();                // the store must have read the buffer
+                issue(k + STAGES);
             }
         }
         __syncwarp();
-        if (lane == 0 && k + STAGES < nst) {
-            fence_proxy_async_smem();
-            issue(k + STAGES);
-        }
     }
+    if (lane == 0) bulk_wait0();
     if (timed_out) {
         // drain the boxes still in flight (bounded), then report
         const int last = min(kfail + STAGES, nst);

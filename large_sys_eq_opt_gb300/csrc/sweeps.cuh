@@ -214,8 +214,8 @@ __device__ __forceinline__ void warp_arrive(Ctl* ctl, T smax, bool bad, bool tim
 // x-sweep: Uold (S buffer) -> Utmp.  One warp per (32-row group, x-segment),
 // one row per lane.  src/cpu/solver_cpu.cpp:206-238 + :437-461
 //
-// Box k holds S columns [m0 + 8k, m0 + 8k + 8) of 32 rows (m0 = s0 - 4 in
-// FP32 units of 32 bytes).  The cell updated when S column c is pushed is
+// Box k holds S columns [m0 + CX k, m0 + CX (k+1)) of 32 rows, CX = 32 bytes
+// of columns, m0 = s0 + 4 - CX.  The cell updated when S column c is pushed is
 // interior column c - 4, which sits in Utmp column c: every output lands in
 // the shared-memory slot its input came from, so the box is overwritten in
 // place and written back with one TMA store.  Box 0 only warms the stencil
@@ -245,7 +245,8 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     const int rg = task / a.nseg;                // 32-row group
     const int s0 = (task - rg * a.nseg) * a.seg; // first interior column of the segment
     const int e = min(s0 + a.seg, a.nx);
-    const int m0 = s0 - HV;                      // first S column marched (4 FP32 / 2 FP64 cells early)
+    const int m0 = s0 + 4 - CX;                  // first S column marched: box k >= 1 holds outputs
+                                                 // [s0 + CX(k-1), s0 + CX k) (FP32: 4 columns early)
     const int nst = 1 + (e - s0 + CX - 1) / CX;  // warm-up box + output boxes
     const int j = rg * 32 + lane;                // interior row of this lane
     const bool row_ok = j < a.ny;

@@ -151,16 +151,16 @@ int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long 
 
 int encode_all(eu_handle* h) {
     for (int b = 0; b < 2; ++b)
-        if (int rc = encode(h, &h->tm_x[b], h->S[b], h->cfg.nx + 4, h->pitch_s, h->plane_s, h->K.box_x, 32,
+        if (int rc = encode(h, &h->tm_x[b], h->S[b], h->cfg.nx + kSOff + 2, h->pitch_s, h->plane_s, h->K.box_x, 32,
                             CU_TENSOR_MAP_SWIZZLE_32B, h->l2promo_x))
             return rc;
     // x-sweep stores: width nx+4 and height ny+2 clip everything past the
     // last interior column / row, so no box spills into the top ghost rows.
-    if (int rc = encode(h, &h->tm_xo, h->Tm, h->cfg.nx + 4, h->pitch_t, h->plane_t, h->K.box_x, 32,
+    if (int rc = encode(h, &h->tm_xo, h->Tm, h->cfg.nx + kTOff, h->pitch_t, h->plane_t, h->K.box_x, 32,
                         CU_TENSOR_MAP_SWIZZLE_32B, 256, h->cfg.ny + 2))
         return rc;
-    return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE,
-                  h->l2promo_y);
+    return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, h->l2promo_y);
 }
 
 // Work decomposition: enough independent warps to fill every SM a few times
@@ -180,8 +180,8 @@ void plan(eu_handle* h) {
     h->nseg_x = (nx + seg - 1) / seg;
     h->ntasks_x = rgroups * h->nseg_x;
     h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
-    // y-sweep: 32 columns per warp, row segments
-    const int groups = (nx + 31) / 32;
+    // y-sweep: 32 S columns per warp, row segments
+    const int groups = (nx + kSOff + 31) / 32;
     int nsy = (int)std::max<long long>((target + groups - 1) / groups, 1);
     int segy = (ny + nsy - 1) / nsy;
     segy = std::max(segy, std::min(ny, 128));
@@ -259,14 +259,14 @@ cudaError_t launch_dt(eu_handle* h, int b) {
 
 cudaError_t unpack_state(eu_handle* h, int b, double* d_aos) {
     if (h->prec == EU_FP32)
-        return launch_unpack_aos<float>(planes_s<float>(h, b), 2, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
-    return launch_unpack_aos<double>(planes_s<double>(h, b), 2, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+        return launch_unpack_aos<float>(planes_s<float>(h, b), kSOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+    return launch_unpack_aos<double>(planes_s<double>(h, b), kSOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
 }
 
 cudaError_t unpack_tmp(eu_handle* h, double* d_aos) {
     if (h->prec == EU_FP32)
-        return launch_unpack_aos<float>(planes_t<float>(h), 4, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
-    return launch_unpack_aos<double>(planes_t<double>(h), 4, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+        return launch_unpack_aos<float>(planes_t<float>(h), kTOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
+    return launch_unpack_aos<double>(planes_t<double>(h), kTOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
 }
 
 cudaError_t fill_ghosts(eu_handle* h, int b) {
@@ -452,8 +452,8 @@ int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limite
         return rc;
     };
     const long long align = 128 / (long long)h->esz;
-    h->pitch_s = round_up(cfg->nx + 4, align);
-    h->pitch_t = round_up(cfg->nx + 8, align);
+    h->pitch_s = round_up(cfg->nx + kSOff + 2, align);
+    h->pitch_t = round_up(cfg->nx + kTOff, align);
     h->plane_s = round_up(h->pitch_s * (cfg->ny + 4), 256 / (long long)h->esz);
     h->plane_t = round_up(h->pitch_t * (cfg->ny + 4), 256 / (long long)h->esz);
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
@@ -727,10 +727,10 @@ int eu_get_time(eu_handle* h, double* t, long long* steps, double* dt_next) {
 int eu_totals(eu_handle* h, double out[4]) {
     if (!h || !out) return fail(h, EU_ERR_INVALID, "null argument");
     if (h->prec == EU_FP32)
-        EU_CUDA(h, launch_totals<float>(planes_s<float>(h, h->cur), 2, h->cfg.nx, h->cfg.ny, h->d_part, h->part_blocks,
-                                        h->d_tot, h->st));
+        EU_CUDA(h, launch_totals<float>(planes_s<float>(h, h->cur), kSOff, h->cfg.nx, h->cfg.ny, h->d_part,
+                                        h->part_blocks, h->d_tot, h->st));
     else
-        EU_CUDA(h, launch_totals<double>(planes_s<double>(h, h->cur), 2, h->cfg.nx, h->cfg.ny, h->d_part,
+        EU_CUDA(h, launch_totals<double>(planes_s<double>(h, h->cur), kSOff, h->cfg.nx, h->cfg.ny, h->d_part,
                                          h->part_blocks, h->d_tot, h->st));
     EU_CUDA(h, cudaMemcpyAsync(h->h_tot, h->d_tot, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     EU_CUDA(h, cudaStreamSynchronize(h->st));

@@ -34,7 +34,7 @@ __global__ void pack_aos_kernel(const double* __restrict__ aos, Planes<T> P, int
         const long long r = idx / tnx, c = idx - r * tnx;
         const double2 u01 = reinterpret_cast<const double2*>(aos)[2 * idx];
         const double2 u23 = reinterpret_cast<const double2*>(aos)[2 * idx + 1];
-        T* q = P.base + r * P.pitch + c;
+        T* q = P.base + r * P.pitch + (c + kSOff - 2);
         q[0] = T(u01.x); q[P.plane] = T(u01.y); q[2 * P.plane] = T(u23.x); q[3 * P.plane] = T(u23.y);
     }
 }
@@ -74,8 +74,8 @@ __global__ void fill_ghosts_kernel(Planes<T> P, int nx, int ny, int4 bc) {
         bool fx, fy;
         const int si = ghost_src(c, nx, bc.x, bc.y, fx);
         const int sj = ghost_src(r, ny, bc.z, bc.w, fy);
-        const T* q = P.base + (long long)(sj + 2) * P.pitch + (si + 2);
-        T* o = P.base + (long long)r * P.pitch + c;
+        const T* q = P.base + (long long)(sj + 2) * P.pitch + (si + kSOff);
+        T* o = P.base + (long long)r * P.pitch + (c + kSOff - 2);
         o[0] = q[0];
         o[P.plane] = fx ? -q[P.plane] : q[P.plane];
         o[2 * P.plane] = fy ? -q[2 * P.plane] : q[2 * P.plane];
@@ -118,7 +118,7 @@ __device__ __forceinline__ double cell_centre(double lo, int idx, double d) {
 
 template <class T>
 __device__ __forceinline__ void put(Planes<T> P, int r, int c, Cell4 u) {
-    T* q = P.base + (long long)r * P.pitch + c;
+    T* q = P.base + (long long)r * P.pitch + (c + kSOff - 2);
     q[0] = T(u.r); q[P.plane] = T(u.mu); q[2 * P.plane] = T(u.mv); q[3 * P.plane] = T(u.e);
 }
 
@@ -173,7 +173,7 @@ __global__ void dt_kernel(Planes<T> P, int nx, int ny, Ctl* ctl, unsigned int nw
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
         const long long j = idx / nx, i = idx - j * nx;
-        const T* q = P.base + (j + 2) * P.pitch + (i + 2);
+        const T* q = P.base + (j + 2) * P.pitch + (i + kSOff);
         const Cons<T> U{q[0], q[P.plane], q[2 * P.plane], q[3 * P.plane]};
         const T sp = max_signal_speed(U);
         bad |= !(sp < T(INFINITY));

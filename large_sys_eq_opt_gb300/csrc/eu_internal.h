@@ -45,6 +45,14 @@ struct Ctl {
 enum { kModeCfl = 0, kModeFrozen = 1, kModeHost = 2 };
 enum { kStatusOk = 0, kStatusNonPhysical = 1, kStatusTimeout = 2, kStatusNonFinite = 4 };
 
+// Column of interior cell i in the state buffers S0/S1 (ghosts at i+4, i+5
+// and nx+6, nx+7; columns 0-3 unused) and in Utmp.  With these offsets
+// every TMA box and every warp-wide row store of both sweeps starts on a
+// 32-byte sector boundary, so DRAM never sees a partial-sector write (which
+// costs an ECC read-modify-write).
+constexpr int kSOff = 6;
+constexpr int kTOff = 8;
+
 // SoA plane set: field f (0 rho, 1 rhou, 2 rhov, 3 E), array row r, column c
 // at base[f*plane + r*pitch + c].
 template <class T> struct Planes {
@@ -57,7 +65,7 @@ template <class T> struct Planes {
 enum { kBcTransmissive = 0, kBcReflective = 1 };
 
 template <class T> struct SweepArgs {
-    Planes<T> out;       // x-sweep: Utmp (interior at col+4,row+2); y-sweep: Unew (col+2,row+2)
+    Planes<T> out;       // x-sweep: Utmp (interior at col+kTOff, row+2); y-sweep: Unew (col+kSOff, row+2)
     Ctl* ctl;
     int nx, ny;
     int seg;             // outputs per task along the march direction
@@ -78,7 +86,8 @@ using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const CUtensorMap* tm
 struct SweepKernels {
     SweepLaunch x, y;
     int box_x;           // x-sweep box: box_x columns (32 bytes) x 32 rows, 32-byte swizzle
-    int ry;              // y-sweep box: 32 columns x ry rows
+    int ry;              // y-sweep box: box_w_y columns x ry rows
+    int box_w_y;
     int stages_x, stages_y;
     int nw;              // warps per CTA
     size_t smem_x, smem_y;

@@ -35,10 +35,11 @@ constexpr int MINB_X = 2, MINB_Y = 2;
 constexpr int CX = 32 / sizeof(T);
 constexpr int SX = 3;
 constexpr int RY = 4, SY = 3;
+constexpr int BWY = 36;                 // y-sweep box width: the warp's 32 columns + 2, rounded to 16 B
 constexpr int NW = 4;
 constexpr int SOL = EU_SOLVER;
 constexpr size_t kStageX = 4 * 32 * CX * sizeof(T);
-constexpr size_t kStageY = 4 * RY * 32 * sizeof(T);
+constexpr size_t kStageY = (4 * RY * BWY * sizeof(T) + 127) / 128 * 128;
 constexpr size_t kSmemX = 1024 + NW * SX * kStageX + NW * SX * sizeof(uint64_t);
 constexpr size_t kSmemY = 1024 + NW * SY * kStageY + NW * SY * sizeof(uint64_t);
 
@@ -53,7 +54,7 @@ static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, co
 
 static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap*, const void* args, int ctas,
                             cudaStream_t s) {
-    auto k = sweep_y_kernel<T, SOL, RY, SY, NW, MINB_Y>;
+    auto k = sweep_y_kernel<T, SOL, RY, BWY, SY, NW, MINB_Y>;
     static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
     if (attr != cudaSuccess) return attr;
     k<<<ctas, NW * 32, kSmemY, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
@@ -68,6 +69,7 @@ SweepKernels EU_NAME(sweep_kernels, EU_PREC, EU_SOLVER)() {
     k.y = LAUNCH_Y;
     k.box_x = CX;
     k.ry = RY;
+    k.box_w_y = BWY;
     k.stages_x = SX;
     k.stages_y = SY;
     k.nw = NW;

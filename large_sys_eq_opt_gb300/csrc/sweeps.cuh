@@ -2,10 +2,12 @@
 // step (src/cpu/solver_cpu.cpp:400-499 restated for sm_103a).
 //
 // Data layout in HBM (SoA planes, 2-cell ghost frame):
-//   state buffers S0/S1 : interior (i, j) at column i+2, row j+2
-//   Utmp                : interior (i, j) at column i+4, row j+2
+//   state buffers S0/S1 : interior (i, j) at column i+kSOff (6), row j+2
+//   Utmp                : interior (i, j) at column i+kTOff (8), row j+2
 // The x-sweep finalises a cell two cells behind the newest one it reads; the
-// extra two columns of Utmp turn that lag into an aligned 16-byte store.
+// two extra columns of Utmp put each output in the Utmp column equal to the
+// S column of the newest input, and both offsets keep every box and every
+// warp-wide row store on a 32-byte sector boundary.
 //
 // Execution model: every lane owns one grid line (a row in the x-sweep, a
 // column in the y-sweep) and marches along it; the 5-cell stencil window
@@ -215,11 +217,12 @@ __device__ __forceinline__ void warp_arrive(Ctl* ctl, T smax, bool bad, bool tim
 // one row per lane.  src/cpu/solver_cpu.cpp:206-238 + :437-461
 //
 // Box k holds S columns [m0 + CX k, m0 + CX (k+1)) of 32 rows, CX = 32 bytes
-// of columns, m0 = s0 + 4 - CX.  The cell updated when S column c is pushed is
-// interior column c - 4, which sits in Utmp column c: every output lands in
-// the shared-memory slot its input came from, so the box is overwritten in
-// place and written back with one TMA store.  Box 0 only warms the stencil
-// window up; boxes 1..seg/CX hold exactly this segment's outputs.
+// of columns, m0 = s0 + kSOff + 2 - CX.  The cell updated when S column c is
+// pushed is interior column c - kSOff - 2, which sits in Utmp column c:
+// every output lands in the shared-memory slot its input came from, so the
+// box is overwritten in place and written back with one TMA store of whole
+// 32-byte rows.  Box 0 only warms the stencil window up; boxes 1.. hold
+// exactly this segment's outputs (clipped by the store map at the edges).
 // ---------------------------------------------------------------------------
 template <class T, int S, int STAGES, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB)
@@ -230,6 +233,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     constexpr int STAGE = 4 * 32 * CX;          // elements: 4 fields x 32 rows x CX
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
     static_assert(STAGE_BYTES % 1024 == 0, "32-byte swizzle needs 1 KB-aligned stage buffers");
+    static_assert(kTOff == kSOff + 2, "outputs must land in their input's column");
     extern __shared__ __align__(1024) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int task = blockIdx.x * NW + warp;
@@ -245,8 +249,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     const int rg = task / a.nseg;                // 32-row group
     const int s0 = (task - rg * a.nseg) * a.seg; // first interior column of the segment
     const int e = min(s0 + a.seg, a.nx);
-    const int m0 = s0 + 4 - CX;                  // first S column marched: box k >= 1 holds outputs
-                                                 // [s0 + CX(k-1), s0 + CX k) (FP32: 4 columns early)
+    const int m0 = s0 + kSOff + 2 - CX;          // first S column marched
     const int nst = 1 + (e - s0 + CX - 1) / CX;  // warm-up box + output boxes
     const int j = rg * 32 + lane;                // interior row of this lane
     const bool row_ok = j < a.ny;
@@ -278,7 +281,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     // transmissive sides copy the edge row into both layers, reflective
     // sides mirror rows 0/1 (ny-1/ny-2) with rho*v negated.  At most four.
     int g0 = -1, g1 = -1, g2 = -1, g3 = -1;
-    bool n0 = false, n1 = false, n2 = false, n3 = false;
+    bool n0 = false, n2 = false;
     if (row_ok) {
         if (a.bc_lo == kBcReflective) {
             if (j == 0) { g0 = 1; n0 = true; }
@@ -308,6 +311,17 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             break;
         }
         T* rowp = buf + s * STAGE + lane * CX;
+        if (snap && row_ok) {                    // the input state is a requested snapshot
+            for (int c = 0; c < CX; ++c) {
+                const int is = m0 + k * CX + c - kSOff;
+                if (is >= s0 && is < e) {
+                    const T* q = rowp + (((c / HV) ^ swz) * HV) + (c % HV);
+                    T* p = snap + (long long)j * a.nx + is;
+                    p[0] = q[0]; p[a.snap_plane] = q[32 * CX]; p[2 * a.snap_plane] = q[64 * CX];
+                    p[3 * a.snap_plane] = q[96 * CX];
+                }
+            }
+        }
 #pragma unroll 1
         for (int h = 0; h < 2; ++h) {
             T* q = rowp + ((h ^ swz) * HV);
@@ -316,33 +330,27 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             ld_vec<T, HV>(q + 32 * CX, mn);
             ld_vec<T, HV>(q + 64 * CX, mt);
             ld_vec<T, HV>(q + 96 * CX, en);
-            const int c0 = m0 + k * CX + h * HV;  // S (and Utmp) column of the first cell
 #pragma unroll
             for (int v = 0; v < HV; ++v) {
-                const Cons<T> U{r[v], mn[v], mt[v], en[v]};
-                if (snap && row_ok) {             // the input state is a requested snapshot
-                    const int is = c0 + v - 2;
-                    if (is >= s0 && is < e) {
-                        T* p = snap + (long long)j * a.nx + is;
-                        p[0] = U.r; p[a.snap_plane] = U.mn; p[2 * a.snap_plane] = U.mt; p[3 * a.snap_plane] = U.e;
-                    }
-                }
-                const Cons<T> N = line.push(U, hl, lam);
+                const Cons<T> N = line.push(Cons<T>{r[v], mn[v], mt[v], en[v]}, hl, lam);
                 r[v] = N.r; mn[v] = N.mn; mt[v] = N.mt; en[v] = N.e;
-                if (has_ghost && k > 0) {
-                    const int ic = c0 + v - 4;
-                    if (ic >= s0 && ic < e) {
-                        if (g0 >= 0) store_cell(a.out, g0, c0 + v, N, 1, 2, n0);
-                        if (g1 >= 0) store_cell(a.out, g1, c0 + v, N, 1, 2, n1);
-                        if (g2 >= 0) store_cell(a.out, g2, c0 + v, N, 1, 2, n2);
-                        if (g3 >= 0) store_cell(a.out, g3, c0 + v, N, 1, 2, n3);
-                    }
-                }
             }
             st_vec<T, HV>(q, r);                  // outputs overwrite their inputs in place
             st_vec<T, HV>(q + 32 * CX, mn);
             st_vec<T, HV>(q + 64 * CX, mt);
             st_vec<T, HV>(q + 96 * CX, en);
+        }
+        if (has_ghost && k > 0) {                 // y-ghost rows of Utmp (few lanes)
+            for (int c = 0; c < CX; ++c) {
+                const int col = m0 + k * CX + c;
+                if (col - kTOff >= a.nx) break;
+                const T* q = rowp + (((c / HV) ^ swz) * HV) + (c % HV);
+                const Cons<T> N{q[0], q[32 * CX], q[64 * CX], q[96 * CX]};
+                if (g0 >= 0) store_cell(a.out, g0, col, N, 1, 2, n0);
+                if (g1 >= 0) store_cell(a.out, g1, col, N, 1, 2, false);
+                if (g2 >= 0) store_cell(a.out, g2, col, N, 1, 2, n2);
+                if (g3 >= 0) store_cell(a.out, g3, col, N, 1, 2, false);
+            }
         }
         fence_proxy_async_smem();                 // make the in-place writes visible to TMA
         __syncwarp();
@@ -351,9 +359,10 @@ __global__ void __launch_bounds__(NW * 32, MINB)
                 tma_store_3d(&tm_out, smem_u32(buf + s * STAGE), m0 + k * CX, rg * 32 + 2, 0);
                 bulk_commit();
             }
-            if (k + STAGES < nst) {
-                bulk_wait_read0();                // the store must have read the buffer
-                issue(k + STAGES);
+            // refill the buffer of box k-1 (its store, if any, is the older group)
+            if (k > 0 && k - 1 + STAGES < nst) {
+                bulk_wait_read1();
+                issue(k - 1 + STAGES);
             }
         }
         __syncwarp();
@@ -370,13 +379,15 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 
 // ---------------------------------------------------------------------------
 // y-sweep: Utmp -> Unew (S buffer), with the fused CFL reduction.  One warp
-// per (row segment, 32-column group), one column per lane.
-// src/cpu/solver_cpu.cpp:247-279 + :474-498
+// per (row segment, group of 32 S columns), one column per lane; the box is
+// BW >= 34 Utmp columns wide because Utmp's interior sits two columns right
+// of the S interior.  src/cpu/solver_cpu.cpp:247-279 + :474-498
 // ---------------------------------------------------------------------------
-template <class T, int S, int RY, int STAGES, int NW, int MINB>
+template <class T, int S, int RY, int BW, int STAGES, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB)
     sweep_y_kernel(const __grid_constant__ CUtensorMap tm, const SweepArgs<T> a) {
-    constexpr int STAGE = 4 * RY * 32;
+    constexpr int STAGE = 4 * RY * BW;
+    static_assert(BW >= 32 + kTOff - kSOff, "box too narrow");
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
     static_assert(STAGE_BYTES % 128 == 0, "stage buffers must stay 128-byte aligned");
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -391,12 +402,13 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
 
     const int rs = task / a.nseg;                // row segment
-    const int g = task - rs * a.nseg;            // 32-column group
+    const int g = task - rs * a.nseg;            // group of 32 S columns
     const int r0 = rs * a.seg;                   // first interior output row
     const int e = min(r0 + a.seg, a.ny);
     const int nst = (e + 4 - r0 + RY - 1) / RY;  // boxes: Utmp rows [r0, e+4)
-    const int i = g * 32 + lane;                 // interior column of this lane
-    const bool col_ok = i < a.nx;
+    const int sc = g * 32 + lane;                // S column of this lane
+    const int i = sc - kSOff;                    // its interior column
+    const bool col_ok = i >= 0 && i < a.nx;
     const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dy
     const T lam = T(lam_d);
     const T hl = T(0.5 * lam_d);
@@ -411,7 +423,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         const int s = k % STAGES;
         const uint32_t b = smem_u32(&bar[s]);
         mbar_arrive_expect_tx(b, STAGE_BYTES);
-        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, g * 32 + 4, r0 + k * RY, 0);
+        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, g * 32, r0 + k * RY, 0);
     };
     if (lane == 0) {
         const int np = min(STAGES, nst);
@@ -430,32 +442,32 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             kfail = k;
             break;
         }
-        const T* sb = buf + s * STAGE + lane;
+        const T* sb = buf + s * STAGE + lane + (kTOff - kSOff);
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
             // normal momentum of the y-sweep is rho*v (plane 2)
-            const Cons<T> U{sb[rr * 32], sb[(2 * RY + rr) * 32], sb[(RY + rr) * 32], sb[(3 * RY + rr) * 32]};
+            const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
             const Cons<T> N = line.push(U, hl, lam);
             const int ir = r0 + k * RY + rr - 4;  // interior row of N
             if (ir >= r0 && ir < e && col_ok) {
-                store_cell(a.out, ir + 2, i + 2, N, 2, 1, false);
+                store_cell(a.out, ir + 2, sc, N, 2, 1, false);
                 const T sp = max_signal_speed(N);
                 bad |= !(sp < T(INFINITY));
                 smax = Ar<T>::fmax_(smax, sp);
                 // x-ghost columns of Unew read by the next x-sweep
                 if (i == 0) {
-                    if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, 1, N, 2, 1, true);
-                    else { store_cell(a.out, ir + 2, 1, N, 2, 1, false);
-                           store_cell(a.out, ir + 2, 0, N, 2, 1, false); }
+                    if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
+                    else { store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, false);
+                           store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, false); }
                 }
-                if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, 0, N, 2, 1, true);
+                if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, true);
                 if (i == a.nx - 1) {
-                    if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + 2, N, 2, 1, true);
-                    else { store_cell(a.out, ir + 2, a.nx + 2, N, 2, 1, false);
-                           store_cell(a.out, ir + 2, a.nx + 3, N, 2, 1, false); }
+                    if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, true);
+                    else { store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, false);
+                           store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, false); }
                 }
                 if (i == a.nx - 2 && a.bc_hi == kBcReflective)
-                    store_cell(a.out, ir + 2, a.nx + 3, N, 2, 1, true);
+                    store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, true);
             }
         }
         __syncwarp();

@@ -163,31 +163,48 @@ int encode_all(eu_handle* h) {
                   CU_TENSOR_MAP_SWIZZLE_NONE, h->l2promo_y);
 }
 
-// Work decomposition: enough independent warps to fill every SM a few times
-// over, with segments long enough that the 4-cell halo per segment stays a
-// small fraction of the work.
+// Work decomposition.  Every warp is one task; a launch runs in
+// ceil(tasks / slots) waves, slots = SMs x resident warps per SM.  The
+// segment length is chosen to minimise waves x (segment + warm-up), so the
+// last wave is nearly full and the per-segment warm-up (4 cells, plus one
+// box in the x-sweep) stays a small fraction of the work.  A launch that
+// fills less than one wave is costed by its fill fraction, floored at a
+// quarter (below that the warps are latency-bound, not issue-bound).
+double waves_of(long long tasks, long long slots) {
+    if (tasks <= slots) return std::max((double)tasks / (double)slots, 0.25);
+    return (double)((tasks + slots - 1) / slots);
+}
+
 void plan(eu_handle* h) {
     const int nx = h->cfg.nx, ny = h->cfg.ny;
-    const long long target = (long long)h->sm_count * 32;   // warps: ~2 resident waves
+    const long long slots_x = (long long)h->sm_count * h->K.nw * h->K.occ_x();
+    const long long slots_y = (long long)h->sm_count * h->K.nw * h->K.occ_y();
     // x-sweep: 32 rows per warp, segments of whole boxes along x
     const int rgroups = (ny + 31) / 32;
     const int CX = h->K.box_x;
-    const int max_seg = (nx + CX - 1) / CX;
-    int nseg = (int)std::min<long long>(std::max<long long>((target + rgroups - 1) / rgroups, 1), max_seg);
-    int seg = (int)round_up((nx + nseg - 1) / nseg, CX);
-    seg = std::max(seg, (int)std::min<long long>(round_up(nx, CX), 256));  // keep the 4-cell warm-up small
-    h->seg_x = seg;
-    h->nseg_x = (nx + seg - 1) / seg;
+    const int nboxes = (nx + CX - 1) / CX;
+    double best = 1e300;
+    for (int nseg = 1; nseg <= nboxes; ++nseg) {
+        const int seg = (int)round_up((nx + nseg - 1) / nseg, CX);
+        const int ns = (nx + seg - 1) / seg;
+        if (ns != nseg) continue;
+        const double cost = waves_of(rgroups * (long long)ns, slots_x) * (seg + CX + 4);
+        if (cost < best * 0.999) { best = cost; h->seg_x = seg; h->nseg_x = ns; }
+    }
     h->ntasks_x = rgroups * h->nseg_x;
     h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
     // y-sweep: 32 S columns per warp, row segments
     const int groups = (nx + kSOff + 31) / 32;
-    int nsy = (int)std::max<long long>((target + groups - 1) / groups, 1);
-    int segy = (ny + nsy - 1) / nsy;
-    segy = std::max(segy, std::min(ny, 128));
-    h->seg_y = segy;
+    best = 1e300;
+    for (int nseg = 1; nseg <= ny; ++nseg) {
+        const int seg = (ny + nseg - 1) / nseg;
+        if ((ny + seg - 1) / seg != nseg) continue;
+        const double cost = waves_of(groups * (long long)nseg, slots_y) * (seg + 4);
+        if (cost < best * 0.999) { best = cost; h->seg_y = seg; }
+        if (seg <= 16) break;
+    }
     h->nseg_y = groups;  // tasks per row segment
-    h->ntasks_y = groups * ((ny + segy - 1) / segy);
+    h->ntasks_y = groups * ((ny + h->seg_y - 1) / h->seg_y);
     h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
 }
 

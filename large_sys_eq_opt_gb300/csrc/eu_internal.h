@@ -85,6 +85,8 @@ using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const CUtensorMap* tm
 
 struct SweepKernels {
     SweepLaunch x, y;
+    int (*occ_x)();      // resident CTAs per SM of each kernel
+    int (*occ_y)();
     int box_x;           // x-sweep box: box_x columns (32 bytes) x 32 rows, 32-byte swizzle
     int ry;              // y-sweep box: box_w_y columns x ry rows
     int box_w_y;

@@ -16,6 +16,8 @@
 #define EU_NAME(base, p, s) EU_NAME2(base, p, s)
 #define LAUNCH_X EU_NAME(launch_x, EU_PREC, EU_SOLVER)
 #define LAUNCH_Y EU_NAME(launch_y, EU_PREC, EU_SOLVER)
+#define OCC_X EU_NAME(occ_x, EU_PREC, EU_SOLVER)
+#define OCC_Y EU_NAME(occ_y, EU_PREC, EU_SOLVER)
 
 namespace eu {
 namespace {
@@ -61,12 +63,30 @@ static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap*, const voi
     return cudaGetLastError();
 }
 
+static int OCC_X() {
+    auto k = sweep_x_kernel<T, SOL, SX, NW, MINB_X>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, kSmemX) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+static int OCC_Y() {
+    auto k = sweep_y_kernel<T, SOL, RY, BWY, SY, NW, MINB_Y>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, kSmemY) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
 }  // namespace
 
 SweepKernels EU_NAME(sweep_kernels, EU_PREC, EU_SOLVER)() {
     SweepKernels k;
     k.x = LAUNCH_X;
     k.y = LAUNCH_Y;
+    k.occ_x = OCC_X;
+    k.occ_y = OCC_Y;
     k.box_x = CX;
     k.ry = RY;
     k.box_w_y = BWY;

@@ -163,46 +163,31 @@ int encode_all(eu_handle* h) {
                   CU_TENSOR_MAP_SWIZZLE_NONE, h->l2promo_y);
 }
 
-// Work decomposition.  Every warp is one task; a launch runs in
-// ceil(tasks / slots) waves, slots = SMs x resident warps per SM.  The
-// segment length is chosen to minimise waves x (segment + warm-up), so the
-// last wave is nearly full and the per-segment warm-up (4 cells, plus one
-// box in the x-sweep) stays a small fraction of the work.  A launch that
-// fills less than one wave is costed by its fill fraction, floored at a
-// quarter (below that the warps are latency-bound, not issue-bound).
-double waves_of(long long tasks, long long slots) {
-    if (tasks <= slots) return std::max((double)tasks / (double)slots, 0.25);
-    return (double)((tasks + slots - 1) / slots);
-}
-
+// Work decomposition.  Every warp is one task: a segment of one group of 32
+// lines.  Measured on GB300 (8192^2 and 2048^2, FP32 HLLC), launches of many
+// short tasks beat near-single-wave launches of long ones even though each
+// task recomputes a 4-cell warm-up (plus one box in the x-sweep): CTAs refill
+// the SMs as they retire, the tail shrinks to one short task, and fewer
+// lines are in flight at once.  The default aims at about eight tasks per
+// resident warp slot with segments clamped to [32, 128] rows (y) and
+// [32, 256] columns (x); eu_set_option overrides it.
 void plan(eu_handle* h) {
     const int nx = h->cfg.nx, ny = h->cfg.ny;
     const long long slots_x = (long long)h->sm_count * h->K.nw * h->K.occ_x();
     const long long slots_y = (long long)h->sm_count * h->K.nw * h->K.occ_y();
-    // x-sweep: 32 rows per warp, segments of whole boxes along x
-    const int rgroups = (ny + 31) / 32;
     const int CX = h->K.box_x;
-    const int nboxes = (nx + CX - 1) / CX;
-    double best = 1e300;
-    for (int nseg = 1; nseg <= nboxes; ++nseg) {
-        const int seg = (int)round_up((nx + nseg - 1) / nseg, CX);
-        const int ns = (nx + seg - 1) / seg;
-        if (ns != nseg) continue;
-        const double cost = waves_of(rgroups * (long long)ns, slots_x) * (seg + CX + 4);
-        if (cost < best * 0.999) { best = cost; h->seg_x = seg; h->nseg_x = ns; }
-    }
+    const int rgroups = (ny + 31) / 32;
+    long long want = ((long long)rgroups * nx + 8 * slots_x - 1) / (8 * slots_x);
+    want = std::min<long long>(std::max<long long>(want, 32), 256);
+    int seg = (int)round_up(std::min<long long>(want, nx), CX);
+    h->seg_x = seg;
+    h->nseg_x = (nx + seg - 1) / seg;
     h->ntasks_x = rgroups * h->nseg_x;
     h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
-    // y-sweep: 32 S columns per warp, row segments
     const int groups = (nx + kSOff + 31) / 32;
-    best = 1e300;
-    for (int nseg = 1; nseg <= ny; ++nseg) {
-        const int seg = (ny + nseg - 1) / nseg;
-        if ((ny + seg - 1) / seg != nseg) continue;
-        const double cost = waves_of(groups * (long long)nseg, slots_y) * (seg + 4);
-        if (cost < best * 0.999) { best = cost; h->seg_y = seg; }
-        if (seg <= 16) break;
-    }
+    want = ((long long)groups * ny + 8 * slots_y - 1) / (8 * slots_y);
+    want = std::min<long long>(std::max<long long>(want, 32), 128);
+    h->seg_y = (int)std::min<long long>(want, ny);
     h->nseg_y = groups;  // tasks per row segment
     h->ntasks_y = groups * ((ny + h->seg_y - 1) / h->seg_y);
     h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
@@ -934,6 +919,9 @@ int eu_get_option(eu_handle* h, const char* name, long long* value) {
     else if (k == "seg_y") *value = h->seg_y;
     else if (k == "graph_steps") *value = h->gsteps;
     else if (k == "tasks_x") *value = h->ntasks_x;
+    else if (k == "occ_x") *value = h->K.occ_x();
+    else if (k == "occ_y") *value = h->K.occ_y();
+    else if (k == "sm_count") *value = h->sm_count;
     else if (k == "tasks_y") *value = h->ntasks_y;
     else return fail(h, EU_ERR_INVALID, "unknown option " + k);
     return EU_OK;

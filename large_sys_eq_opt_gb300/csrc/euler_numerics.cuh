@@ -418,11 +418,16 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
 }
 
 // ---------------------------------------------------------------------------
-// Fast path.  The common case of every branch above, computed straight-line;
-// `slow` is set whenever any of the reference's fallback branches (or the
-// FP64 pressure island) could change the result.  A lane with `slow` set
-// recomputes the cell with the full functions above, so results equal the
-// full path bit for bit while the hot loop carries no fallback code.
+// Fast path.  The common case of every branch above, computed straight-line
+// with the arithmetic regrouped for fused multiply-adds; `slow` is set
+// whenever any of the reference's fallback branches (or the FP32 form's FP64
+// pressure island) could change the result, and such a lane recomputes the
+// cell with the full functions above.  Regroupings used (exact in real
+// arithmetic, rounding differs in the last bits):
+//   kinetic energy   rho|u|^2/2 = (m_n u_n + m_t u_t)/2
+//   pressure         p = (g-1) E - (g-1)/2 (m_n u_n + m_t u_t)
+//   half step        U -/+ (dt/2dx)(F_R - F_L) as one FMA per component
+//   HLLC star state  E* = [(S-u) E + (S*-u)(q S* + p)] / (S - S*), q = rho (S-u)
 // ---------------------------------------------------------------------------
 // All four finite (NaN and inf propagate through the sum; a sum that only
 // overflows needs |values| ~ 1e38 / 1e308 and is treated as non-finite).
@@ -437,27 +442,45 @@ template <class T> __device__ __forceinline__ bool phys_recon_fast(const Prim<T>
 template <class T> __device__ __forceinline__ bool phys_riemann_fast(const Prim<T>& V) {
     return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(0);
 }
+// A cell whose limited face states are physical for any minmod slope: with
+// finite neighbours of non-negative rho and p, minmod keeps the face values
+// of rho and p at or above half the centre value, so rho, p > 4e-12 leaves
+// them above the 1e-12 floors (src/cpu/solver_cpu.cpp:83-87).
+template <class T> __device__ __forceinline__ bool nice_cell(const Prim<T>& V) {
+    return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(4.0e-12);
+}
 
 // cons_to_prim without the FP64 island; flags the states that need it.
 template <class T> __device__ __forceinline__ Prim<T> c2p_fast(const Cons<T>& U, bool& slow) {
-    if constexpr (sizeof(T) == 8) {
-        return cons_to_prim(U);
-    } else {
-        Prim<T> V;
-        V.ir = Ar<T>::rcp(U.r);
-        V.r = U.r;
-        V.un = U.mn * V.ir;
-        V.ut = U.mt * V.ir;
-        const T kinetic = T(0.5) * U.r * (V.un * V.un + V.ut * V.ut);
-        V.p = gm1<T>() * (U.e - kinetic);
-        slow |= T(2) * kinetic > U.e;
-        return V;
-    }
+    Prim<T> V;
+    V.ir = Ar<T>::rcp(U.r);
+    V.r = U.r;
+    V.un = U.mn * V.ir;
+    V.ut = U.mt * V.ir;
+    const T t = U.mt * V.ut + U.mn * V.un;             // twice the kinetic energy
+    V.p = gm1<T>() * U.e - T(0.5 * kGm1D) * t;
+    if constexpr (sizeof(T) == 4) slow |= t > U.e;     // kinetic > E/2: FP64 recovery
+    return V;
 }
 
+// Conserved state and normal flux of a face state given in primitives.
+template <class T>
+__device__ __forceinline__ void face_state(const Prim<T>& W, Cons<T>& U, Cons<T>& F) {
+    U.r = W.r;
+    U.mn = W.r * W.un;
+    U.mt = W.r * W.ut;
+    U.e = W.p * inv_gm1<T>() + T(0.5) * (U.mt * W.ut + U.mn * W.un);
+    F.r = U.mn;
+    F.mn = U.mn * W.un + W.p;
+    F.mt = U.mt * W.un;
+    F.e = (U.e + W.p) * W.un;
+}
+
+// Reconstruct the centre cell of (Wm, Wc, Wp) and evolve its face states by
+// half a step.  `nice` must say that all three cells pass nice_cell().
 template <class T>
 __device__ __forceinline__ void reconstruct_fast(const Prim<T>& Wm, const Prim<T>& Wc, const Prim<T>& Wp,
-                                                 T hl, Face<T>& L, Face<T>& R, bool& slow) {
+                                                 T hl, bool nice, Face<T>& L, Face<T>& R, bool& slow) {
     Prim<T> s;
     s.r = minmod(Wc.r - Wm.r, Wp.r - Wc.r);
     s.un = minmod(Wc.un - Wm.un, Wp.un - Wc.un);
@@ -465,29 +488,26 @@ __device__ __forceinline__ void reconstruct_fast(const Prim<T>& Wm, const Prim<T
     s.p = minmod(Wc.p - Wm.p, Wp.p - Wc.p);
     const Prim<T> WL{Wc.r - T(0.5) * s.r, Wc.un - T(0.5) * s.un, Wc.ut - T(0.5) * s.ut, Wc.p - T(0.5) * s.p, T(0)};
     const Prim<T> WR{Wc.r + T(0.5) * s.r, Wc.un + T(0.5) * s.un, Wc.ut + T(0.5) * s.ut, Wc.p + T(0.5) * s.p, T(0)};
-    const bool okW = phys_recon_fast(WL) && phys_recon_fast(WR);
-    const Cons<T> UL = prim_to_cons(WL), UR = prim_to_cons(WR);
-    Cons<T> FL, FR;
-    if constexpr (sizeof(T) == 8) {
-        FL = flux(UL, cons_to_prim(UL));
-        FR = flux(UR, cons_to_prim(UR));
-    } else {
-        FL = flux(UL, WL);
-        FR = flux(UR, WR);
-    }
-    const Cons<T> h{hl * (FR.r - FL.r), hl * (FR.mn - FL.mn), hl * (FR.mt - FL.mt), hl * (FR.e - FL.e)};
-    L.U = Cons<T>{UL.r - h.r, UL.mn - h.mn, UL.mt - h.mt, UL.e - h.e};
-    R.U = Cons<T>{UR.r - h.r, UR.mn - h.mn, UR.mt - h.mt, UR.e - h.e};
+    Cons<T> UL, FL, UR, FR;
+    face_state(WL, UL, FL);
+    face_state(WR, UR, FR);
+    const T dr = FR.r - FL.r, dmn = FR.mn - FL.mn, dmt = FR.mt - FL.mt, de = FR.e - FL.e;
+    L.U = Cons<T>{UL.r - hl * dr, UL.mn - hl * dmn, UL.mt - hl * dmt, UL.e - hl * de};
+    R.U = Cons<T>{UR.r - hl * dr, UR.mn - hl * dmn, UR.mt - hl * dmt, UR.e - hl * de};
     L.V = c2p_fast(L.U, slow);
     R.V = c2p_fast(R.U, slow);
-    slow |= !(okW && phys_recon_fast(L.V) && phys_recon_fast(R.V));
+    slow |= !(nice && phys_recon_fast(L.V) && phys_recon_fast(R.V));
+}
+
+template <class T> __device__ __forceinline__ Cons<T> nflux(const Cons<T>& U, const Prim<T>& V) {
+    return Cons<T>{U.mn, U.mn * V.un + V.p, U.mt * V.un, (U.e + V.p) * V.un};
 }
 
 // Riemann fluxes for physical inputs (the face states of reconstruct_fast).
 template <class T>
 __device__ __forceinline__ Cons<T> hll_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
                                             const Prim<T>& VR, bool& slow) {
-    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    const Cons<T> FL = nflux(UL, VL), FR = nflux(UR, VR);
     const T aL = sound_speed(VL), aR = sound_speed(VR);
     const T SL = Ar<T>::fmin_(VL.un - aL, VR.un - aR);
     const T SR = Ar<T>::fmax_(VL.un + aL, VR.un + aR);
@@ -505,41 +525,43 @@ __device__ __forceinline__ Cons<T> hll_fast(const Cons<T>& UL, const Prim<T>& VL
 template <class T>
 __device__ __forceinline__ Cons<T> hllc_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
                                              const Prim<T>& VR, bool& slow) {
-    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
     const T aL = sound_speed(VL), aR = sound_speed(VR);
     const T unL = VL.un, unR = VR.un;
     const T SL = Ar<T>::fmin_(unL - aL, unR - aR);
     const T SR = Ar<T>::fmax_(unL + aL, unR + aR);
-    const T qL = VL.r * (SL - unL), qR = VR.r * (SR - unR);
-    const T numerator = VR.p - VL.p + qL * unL - qR * unR;
+    const T sL = SL - unL, sR = SR - unR;
+    const T qL = VL.r * sL, qR = VR.r * sR;
+    const T numerator = (VR.p - VL.p) + qL * unL - qR * unR;
     const T denominator = qL - qR;
     const T Sstar = numerator * Ar<T>::rcp(denominator);
     const bool left = Sstar >= T(0);
     const Cons<T> U = left ? UL : UR;
-    const Cons<T> F = left ? FL : FR;
-    const T rho = left ? VL.r : VR.r;
     const T p = left ? VL.p : VR.p;
     const T un = left ? unL : unR;
     const T ut = left ? VL.ut : VR.ut;
-    const T irho = left ? VL.ir : VR.ir;
     const T S = left ? SL : SR;
+    const T sK = left ? sL : sR;
+    const T q = left ? qL : qR;
+    const Cons<T> F{U.mn, U.mn * un + p, U.mt * un, (U.e + p) * un};
     const T dS = S - Sstar;
-    const T q = rho * (S - un);
-    const T rho_star = q * Ar<T>::rcp(dS);
-    const T E_star = rho_star * (U.e * irho + (Sstar - un) * (Sstar + p * Ar<T>::rcp(q)));
+    const T idS = Ar<T>::rcp(dS);
+    const T rho_star = q * idS;
+    const T E_star = (sK * U.e + (Sstar - un) * (q * Sstar + p)) * idS;
     const Cons<T> Fs{F.r + S * (rho_star - U.r), F.mn + S * (rho_star * Sstar - U.mn),
                      F.mt + S * (rho_star * ut - U.mt), F.e + S * (E_star - U.e)};
     const bool upL = SL >= T(0), upR = SR <= T(0);
     const bool ok = !(Ar<T>::fabs_(denominator) < T(1.0e-14)) && !(Ar<T>::fabs_(dS) < T(1.0e-14)) &&
                     Ar<T>::fabs_(Sstar + rho_star + E_star) < T(INFINITY) && rho_star > T(0);
     slow |= !(upL || upR || ok);
-    return upL ? FL : (upR ? FR : Fs);
+    if (upL) return nflux(UL, VL);
+    if (upR) return nflux(UR, VR);
+    return Fs;
 }
 
 template <class T>
 __device__ __forceinline__ Cons<T> force_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
                                               const Prim<T>& VR, bool& slow) {
-    const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
+    const Cons<T> FL = nflux(UL, VL), FR = nflux(UR, VR);
     const Cons<T> Fc = c_avg(FL, FR);
     const T aL = sound_speed(VL), aR = sound_speed(VR);
     const T alpha = Ar<T>::fmax_(Ar<T>::fabs_(VL.un) + aL, Ar<T>::fabs_(VR.un) + aR);
@@ -552,7 +574,7 @@ __device__ __forceinline__ Cons<T> force_fast(const Cons<T>& UL, const Prim<T>& 
                       Ua.mt - hia * (FR.mt - FL.mt), Ua.e - hia * (FR.e - FL.e)};
     const Prim<T> Vri = c2p_fast(Uri, slow);
     slow |= !(Ar<T>::finite(alpha) && alpha > T(1.0e-14) && phys_riemann_fast(Vri));
-    return c_avg(Flf, flux(Uri, Vri));
+    return c_avg(Flf, nflux(Uri, Vri));
 }
 
 template <int S, class T>
@@ -562,6 +584,16 @@ __device__ __forceinline__ Cons<T> riemann_fast(const Cons<T>& UL, const Prim<T>
     else if constexpr (S == kFORCE) return force_fast(UL, VL, UR, VR, slow);
     else if constexpr (S == kHLL) return hll_fast(UL, VL, UR, VR, slow);
     else return exact_flux(UL, VL, UR, VR);   // the exact solver always takes its full path
+}
+
+// Largest signal speed max(|u|, |v|) + a of a conserved state (the CFL
+// reduction, src/cpu/solver_cpu.cpp:295-300); NaN for a non-finite state.
+template <class T> __device__ __forceinline__ T signal_speed_fast(const Cons<T>& U) {
+    const T ir = Ar<T>::rcp(U.r);
+    const T t = U.mt * U.mt + U.mn * U.mn;
+    const T p = gm1<T>() * U.e - T(0.5 * kGm1D) * (t * ir);
+    const T a = Ar<T>::sqrt_(gam<T>() * p * ir);
+    return Ar<T>::fmax_(Ar<T>::fabs_(U.mn), Ar<T>::fabs_(U.mt)) * ir + a;
 }
 
 // Full-logic recomputation of one cell (out of line; taken only by lanes

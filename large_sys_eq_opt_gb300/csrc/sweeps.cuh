@@ -39,23 +39,26 @@ namespace eu {
 // (head/riemann.hpp:650-672) and cell c-2 is updated with its two face
 // fluxes (src/cpu/solver_cpu.cpp:452-453, :489-490).
 template <class T, int S> struct Line {
-    Prim<T> Wm2, Wm1;   // primitives of cells c-2, c-1
+    Prim<T> Wm2, Wm1;   // primitives of cells c-2, c-1 (1/rho unused)
     Cons<T> Um2, Um1;   // conserved states of cells c-2, c-1
     Face<T> Rp;         // evolved right face state of cell c-2
     Cons<T> Fp;         // flux through face (c-3 | c-2)
+    bool nice2, nice1;  // cells c-2, c-1 pass nice_cell()
     bool rp_phys;       // Rp is physical (always true when it came from the fast path)
 
     __device__ __forceinline__ void reset() {
         Wm2 = Prim<T>{}; Wm1 = Prim<T>{}; Um2 = Cons<T>{}; Um1 = Cons<T>{};
         Rp = Face<T>{}; Fp = Cons<T>{};
+        nice2 = nice1 = false;
         rp_phys = false;
     }
 
     __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
         bool slow = !rp_phys;
         Prim<T> W = c2p_fast(U, slow);
+        const bool nice = nice_cell(W);
         Face<T> L, R;
-        reconstruct_fast(Wm2, Wm1, W, hl, L, R, slow);
+        reconstruct_fast(Wm2, Wm1, W, hl, nice && nice1 && nice2, L, R, slow);
         Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);
         bool r_phys = true;
         if (__builtin_expect(slow, 0)) {
@@ -68,10 +71,12 @@ template <class T, int S> struct Line {
         Wm2 = Wm1; Wm1 = W;
         Um2 = Um1; Um1 = U;
         Rp = R; Fp = F;
+        nice2 = nice1; nice1 = nice;
         rp_phys = r_phys;
         return N;
     }
 };
+
 // Vector loads/stores of VEC consecutive elements (16 B, 8 B or scalar).
 template <class T, int V> __device__ __forceinline__ void ld_vec(const T* p, T (&o)[V]) {
     if constexpr (V == 1) {
@@ -451,7 +456,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             const int ir = r0 + k * RY + rr - 4;  // interior row of N
             if (ir >= r0 && ir < e && col_ok) {
                 store_cell(a.out, ir + 2, sc, N, 2, 1, false);
-                const T sp = max_signal_speed(N);
+                const T sp = signal_speed_fast(N);
                 bad |= !(sp < T(INFINITY));
                 smax = Ar<T>::fmax_(smax, sp);
                 // x-ghost columns of Unew read by the next x-sweep

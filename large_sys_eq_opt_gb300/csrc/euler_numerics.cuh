@@ -54,10 +54,19 @@ template <> struct Ar<double> {
 };
 
 template <> struct Ar<float> {
-    // Approximate reciprocal and square root (max error ~1-2 ulp); the FP32
-    // form is judged against FP64 by its L1/Linf error, not bit-for-bit.
-    static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
-    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    // Hardware approximate reciprocal and square root (PTX rcp.approx /
+    // sqrt.approx, about 1 ulp); the FP32 form is judged against FP64 by its
+    // L1/Linf error, not bit for bit.
+    static __device__ __forceinline__ float rcp(float x) {
+        float y;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+        return y;
+    }
+    static __device__ __forceinline__ float sqrt_(float x) {
+        float y;
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+        return y;
+    }
     static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
     static __device__ __forceinline__ float fmin_(float a, float b) { return fminf(a, b); }
     static __device__ __forceinline__ float fmax_(float a, float b) { return fmaxf(a, b); }
@@ -522,6 +531,13 @@ __device__ __forceinline__ Cons<T> hll_fast(const Cons<T>& UL, const Prim<T>& VL
     return upL ? FL : (upR ? FR : Fh);
 }
 
+// HLLC for physical inputs.  The upwind cases SL >= 0 / SR <= 0 return the
+// flux of the upwind side; that side is also the side of the contact
+// (left iff S* >= 0) whenever the star state is valid (rho* > 0 puts S*
+// strictly inside the fan), so one flux F_K of the side K = left/right of S*
+// serves all three cases: F = F_K + S_eff (U*_K - U_K), S_eff = 0 upwind.
+// Any inconsistency (S* outside the fan, tiny denominators, non-finite
+// star state) flags the lane for the full path.
 template <class T>
 __device__ __forceinline__ Cons<T> hllc_fast(const Cons<T>& UL, const Prim<T>& VL, const Cons<T>& UR,
                                              const Prim<T>& VR, bool& slow) {
@@ -542,20 +558,18 @@ __device__ __forceinline__ Cons<T> hllc_fast(const Cons<T>& UL, const Prim<T>& V
     const T S = left ? SL : SR;
     const T sK = left ? sL : sR;
     const T q = left ? qL : qR;
-    const Cons<T> F{U.mn, U.mn * un + p, U.mt * un, (U.e + p) * un};
     const T dS = S - Sstar;
     const T idS = Ar<T>::rcp(dS);
     const T rho_star = q * idS;
     const T E_star = (sK * U.e + (Sstar - un) * (q * Sstar + p)) * idS;
-    const Cons<T> Fs{F.r + S * (rho_star - U.r), F.mn + S * (rho_star * Sstar - U.mn),
-                     F.mt + S * (rho_star * ut - U.mt), F.e + S * (E_star - U.e)};
     const bool upL = SL >= T(0), upR = SR <= T(0);
+    const T Se = (upL || upR) ? T(0) : S;
     const bool ok = !(Ar<T>::fabs_(denominator) < T(1.0e-14)) && !(Ar<T>::fabs_(dS) < T(1.0e-14)) &&
-                    Ar<T>::fabs_(Sstar + rho_star + E_star) < T(INFINITY) && rho_star > T(0);
-    slow |= !(upL || upR || ok);
-    if (upL) return nflux(UL, VL);
-    if (upR) return nflux(UR, VR);
-    return Fs;
+                    Ar<T>::fabs_(Sstar + rho_star + E_star) < T(INFINITY) && rho_star > T(0) &&
+                    !(upL && !left) && !(upR && left);
+    slow |= !ok;
+    return Cons<T>{U.mn + Se * (rho_star - U.r), (U.mn * un + p) + Se * (rho_star * Sstar - U.mn),
+                   U.mt * un + Se * (rho_star * ut - U.mt), (U.e + p) * un + Se * (E_star - U.e)};
 }
 
 template <class T>
@@ -589,6 +603,7 @@ __device__ __forceinline__ Cons<T> riemann_fast(const Cons<T>& UL, const Prim<T>
 // Largest signal speed max(|u|, |v|) + a of a conserved state (the CFL
 // reduction, src/cpu/solver_cpu.cpp:295-300); NaN for a non-finite state.
 template <class T> __device__ __forceinline__ T signal_speed_fast(const Cons<T>& U) {
+    // head/physics.hpp:39-45 with p from (g-1) E - (g-1)/2 |m|^2 / rho
     const T ir = Ar<T>::rcp(U.r);
     const T t = U.mt * U.mt + U.mn * U.mn;
     const T p = gm1<T>() * U.e - T(0.5 * kGm1D) * (t * ir);

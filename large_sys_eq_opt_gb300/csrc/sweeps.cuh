@@ -437,8 +437,10 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 
     Line<T, S> line;
     line.reset();
-    T smax = T(0);
-    bool bad = false, timed_out = false;
+    T smax = T(0), ssum = T(0);
+    const bool edge = col_ok && (i <= 1 || i >= a.nx - 2);   // writes x-ghost columns
+    const long long pitch = a.out.pitch, plane = a.out.plane;
+    bool timed_out = false;
     int kfail = nst;
     for (int k = 0; k < nst; ++k) {
         const int s = k % STAGES;
@@ -448,31 +450,35 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             break;
         }
         const T* sb = buf + s * STAGE + lane + (kTOff - kSOff);
+        const int ir0 = r0 + k * RY - 4;          // interior row of the first output of this box
+        T* op = a.out.base + (long long)(ir0 + 2) * pitch + sc;
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
             // normal momentum of the y-sweep is rho*v (plane 2)
             const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
             const Cons<T> N = line.push(U, hl, lam);
-            const int ir = r0 + k * RY + rr - 4;  // interior row of N
-            if (ir >= r0 && ir < e && col_ok) {
-                store_cell(a.out, ir + 2, sc, N, 2, 1, false);
+            const int ir = ir0 + rr;
+            if (col_ok && ir >= r0 && ir < e) {
+                T* o = op + rr * pitch;
+                o[0] = N.r; o[plane] = N.mt; o[2 * plane] = N.mn; o[3 * plane] = N.e;
                 const T sp = signal_speed_fast(N);
-                bad |= !(sp < T(INFINITY));
+                ssum += sp;                       // NaN / inf propagate: checked once at the end
                 smax = Ar<T>::fmax_(smax, sp);
-                // x-ghost columns of Unew read by the next x-sweep
-                if (i == 0) {
-                    if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
-                    else { store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, false);
-                           store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, false); }
+                if (edge) {                       // x-ghost columns of Unew read by the next x-sweep
+                    if (i == 0) {
+                        if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
+                        else { store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, false);
+                               store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, false); }
+                    }
+                    if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, true);
+                    if (i == a.nx - 1) {
+                        if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, true);
+                        else { store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, false);
+                               store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, false); }
+                    }
+                    if (i == a.nx - 2 && a.bc_hi == kBcReflective)
+                        store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, true);
                 }
-                if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, true);
-                if (i == a.nx - 1) {
-                    if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, true);
-                    else { store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, false);
-                           store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, false); }
-                }
-                if (i == a.nx - 2 && a.bc_hi == kBcReflective)
-                    store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, true);
             }
         }
         __syncwarp();
@@ -481,6 +487,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             issue(k + STAGES);
         }
     }
+    const bool bad = !(Ar<T>::fabs_(ssum) < T(INFINITY));
     if (timed_out) {
         const int last = min(kfail + STAGES, nst);
         for (int k = kfail + 1; k < last; ++k)

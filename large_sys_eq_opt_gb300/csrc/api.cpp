@@ -87,7 +87,8 @@ struct eu_handle {
     long long dtlog_cap = 0;
     CUtensorMap tm_x[2];
     CUtensorMap tm_y;
-    CUtensorMap tm_xo;   // x-sweep output: Utmp boxes, rows [0, ny+2), columns [0, nx+4)
+    CUtensorMap tm_xo;     // x-sweep output: Utmp boxes, rows [0, ny+2), columns [0, nx+kTOff)
+    CUtensorMap tm_yo[2];  // y-sweep output: S boxes, columns [0, nx+kSOff) (right ghosts clipped)
     SweepKernels K{};
     int seg_x = 0, nseg_x = 0, ntasks_x = 0, ctas_x = 0;
     int seg_y = 0, nseg_y = 0, ntasks_y = 0, ctas_y = 0;
@@ -159,6 +160,10 @@ int encode_all(eu_handle* h) {
     if (int rc = encode(h, &h->tm_xo, h->Tm, h->cfg.nx + kTOff, h->pitch_t, h->plane_t, h->K.box_x, 32,
                         CU_TENSOR_MAP_SWIZZLE_32B, 256, h->cfg.ny + 2))
         return rc;
+    for (int b = 0; b < 2; ++b)
+        if (int rc = encode(h, &h->tm_yo[b], h->S[b], h->cfg.nx + kSOff, h->pitch_s, h->plane_s, 32, h->K.ry,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, 256))
+            return rc;
     return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry,
                   CU_TENSOR_MAP_SWIZZLE_NONE, h->l2promo_y);
 }
@@ -187,7 +192,7 @@ void plan(eu_handle* h) {
     const int groups = (nx + kSOff + 31) / 32;
     want = ((long long)groups * ny + 8 * slots_y - 1) / (8 * slots_y);
     want = std::min<long long>(std::max<long long>(want, 32), 128);
-    h->seg_y = (int)std::min<long long>(want, ny);
+    h->seg_y = (int)round_up(std::min<long long>(want, ny), h->K.ry);  // whole output boxes
     h->nseg_y = groups;  // tasks per row segment
     h->ntasks_y = groups * ((ny + h->seg_y - 1) / h->seg_y);
     h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
@@ -242,10 +247,10 @@ cudaError_t launch_x(eu_handle* h, int cur) {
 cudaError_t launch_y(eu_handle* h, int cur) {
     if (h->prec == EU_FP32) {
         const SweepArgs<float> a = y_args<float>(h, cur);
-        return h->K.y(&h->tm_y, nullptr, &a, h->ctas_y, h->st);
+        return h->K.y(&h->tm_y, &h->tm_yo[1 - cur], &a, h->ctas_y, h->st);
     }
     const SweepArgs<double> a = y_args<double>(h, cur);
-    return h->K.y(&h->tm_y, nullptr, &a, h->ctas_y, h->st);
+    return h->K.y(&h->tm_y, &h->tm_yo[1 - cur], &a, h->ctas_y, h->st);
 }
 
 cudaError_t launch_step(eu_handle* h, int cur) {
@@ -896,7 +901,7 @@ int eu_set_option(eu_handle* h, const char* name, long long value) {
         h->ntasks_x = ((h->cfg.ny + 31) / 32) * h->nseg_x;
         h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
     } else if (k == "seg_y") {
-        if (value < 1) return fail(h, EU_ERR_INVALID, "seg_y must be >= 1");
+        if (value < h->K.ry || value % h->K.ry) return fail(h, EU_ERR_INVALID, "seg_y must be a multiple of the box height");
         h->seg_y = (int)value;
         h->ntasks_y = h->nseg_y * ((h->cfg.ny + h->seg_y - 1) / h->seg_y);
         h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;

@@ -43,7 +43,8 @@ constexpr int SOL = EU_SOLVER;
 constexpr size_t kStageX = 4 * 32 * CX * sizeof(T);
 constexpr size_t kStageY = (4 * RY * BWY * sizeof(T) + 127) / 128 * 128;
 constexpr size_t kSmemX = 1024 + NW * SX * kStageX + NW * SX * sizeof(uint64_t);
-constexpr size_t kSmemY = 1024 + NW * SY * kStageY + NW * SY * sizeof(uint64_t);
+constexpr size_t kOStageY = 4 * RY * 32 * sizeof(T);
+constexpr size_t kSmemY = 1024 + NW * (SY * kStageY + 2 * kOStageY) + NW * SY * sizeof(uint64_t);
 
 static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args, int ctas,
                             cudaStream_t s) {
@@ -54,12 +55,12 @@ static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, co
     return cudaGetLastError();
 }
 
-static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap*, const void* args, int ctas,
+static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args, int ctas,
                             cudaStream_t s) {
     auto k = sweep_y_kernel<T, SOL, RY, BWY, SY, NW, MINB_Y>;
     static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
     if (attr != cudaSuccess) return attr;
-    k<<<ctas, NW * 32, kSmemY, s>>>(*tm, *static_cast<const SweepArgs<T>*>(args));
+    k<<<ctas, NW * 32, kSmemY, s>>>(*tm, *tm_out, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
 }
 

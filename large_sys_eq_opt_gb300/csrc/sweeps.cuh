@@ -40,19 +40,21 @@ namespace eu {
 // fluxes (src/cpu/solver_cpu.cpp:452-453, :489-490).
 template <class T, int S> struct Line {
     Prim<T> Wm2, Wm1;   // primitives of cells c-2, c-1 (1/rho unused)
-    Cons<T> Um2, Um1;   // conserved states of cells c-2, c-1
+    Cons<T> Um1;        // conserved state of cell c-1
+    Cons<T> A;          // U(c-2) + lam F(c-5/2): the update of cell c-2 less its right flux
     Face<T> Rp;         // evolved right face state of cell c-2
-    Cons<T> Fp;         // flux through face (c-3 | c-2)
     bool nice2, nice1;  // cells c-2, c-1 pass nice_cell()
     bool rp_phys;       // Rp is physical (always true when it came from the fast path)
 
     __device__ __forceinline__ void reset() {
-        Wm2 = Prim<T>{}; Wm1 = Prim<T>{}; Um2 = Cons<T>{}; Um1 = Cons<T>{};
-        Rp = Face<T>{}; Fp = Cons<T>{};
+        Wm2 = Prim<T>{}; Wm1 = Prim<T>{}; Um1 = Cons<T>{}; A = Cons<T>{};
+        Rp = Face<T>{};
         nice2 = nice1 = false;
         rp_phys = false;
     }
 
+    // U(c-2) - lam (F(c-3/2) - F(c-5/2)) is evaluated as A - lam F(c-3/2)
+    // (src/cpu/solver_cpu.cpp:452-453, :489-490).
     __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
         bool slow = !rp_phys;
         Prim<T> W = c2p_fast(U, slow);
@@ -66,11 +68,11 @@ template <class T, int S> struct Line {
             W = o.W; L = o.L; R = o.R; F = o.F;
             r_phys = o.r_phys;
         }
-        const Cons<T> N{Um2.r - lam * (F.r - Fp.r), Um2.mn - lam * (F.mn - Fp.mn),
-                        Um2.mt - lam * (F.mt - Fp.mt), Um2.e - lam * (F.e - Fp.e)};
+        const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
+        A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
         Wm2 = Wm1; Wm1 = W;
-        Um2 = Um1; Um1 = U;
-        Rp = R; Fp = F;
+        Um1 = U;
+        Rp = R;
         nice2 = nice1; nice1 = nice;
         rp_phys = r_phys;
         return N;
@@ -282,26 +284,8 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         for (int k = 0; k < np; ++k) issue(k);
     }
 
-    // Ghost rows of Utmp fed by this row (the y-ghosts the y-sweep reads):
-    // transmissive sides copy the edge row into both layers, reflective
-    // sides mirror rows 0/1 (ny-1/ny-2) with rho*v negated.  At most four.
-    int g0 = -1, g1 = -1, g2 = -1, g3 = -1;
-    bool n0 = false, n2 = false;
-    if (row_ok) {
-        if (a.bc_lo == kBcReflective) {
-            if (j == 0) { g0 = 1; n0 = true; }
-            if (j == 1) { g0 = 0; n0 = true; }
-        } else if (j == 0) {
-            g0 = 1; g1 = 0;
-        }
-        if (a.bc_hi == kBcReflective) {
-            if (j == a.ny - 1) { g2 = a.ny + 2; n2 = true; }
-            if (j == a.ny - 2) { g2 = a.ny + 3; n2 = true; }
-        } else if (j == a.ny - 1) {
-            g2 = a.ny + 2; g3 = a.ny + 3;
-        }
-    }
-    const bool has_ghost = g0 >= 0 || g2 >= 0;
+    // rows 0, 1, ny-2, ny-1 also feed the y-ghost rows of Utmp
+    const bool has_ghost = row_ok && (j <= 1 || j >= a.ny - 2);
 
     Line<T, S> line;
     line.reset();
@@ -346,6 +330,22 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             st_vec<T, HV>(q + 96 * CX, en);
         }
         if (has_ghost && k > 0) {                 // y-ghost rows of Utmp (few lanes)
+            // transmissive sides copy the edge row into both ghost layers,
+            // reflective sides mirror rows 0/1 (ny-1/ny-2) with rho*v negated
+            int g0 = -1, g1 = -1, g2 = -1, g3 = -1;
+            bool n0 = false, n2 = false;
+            if (a.bc_lo == kBcReflective) {
+                if (j == 0) { g0 = 1; n0 = true; }
+                if (j == 1) { g0 = 0; n0 = true; }
+            } else if (j == 0) {
+                g0 = 1; g1 = 0;
+            }
+            if (a.bc_hi == kBcReflective) {
+                if (j == a.ny - 1) { g2 = a.ny + 2; n2 = true; }
+                if (j == a.ny - 2) { g2 = a.ny + 3; n2 = true; }
+            } else if (j == a.ny - 1) {
+                g2 = a.ny + 2; g3 = a.ny + 3;
+            }
             for (int c = 0; c < CX; ++c) {
                 const int col = m0 + k * CX + c;
                 if (col - kTOff >= a.nx) break;
@@ -384,17 +384,27 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 
 // ---------------------------------------------------------------------------
 // y-sweep: Utmp -> Unew (S buffer), with the fused CFL reduction.  One warp
-// per (row segment, group of 32 S columns), one column per lane; the box is
-// BW >= 34 Utmp columns wide because Utmp's interior sits two columns right
-// of the S interior.  src/cpu/solver_cpu.cpp:247-279 + :474-498
+// per (row segment, group of 32 S columns), one column per lane; the input
+// box is BW >= 34 Utmp columns wide because Utmp's interior sits two columns
+// right of the S interior.  Box k holds Utmp rows [r0 + 4k, r0 + 4k + 4);
+// a cell is final four rows after it enters, so box k >= 1 yields the output
+// rows [r0 + 4(k-1), r0 + 4k) of this segment (box 0 only warms the window
+// up); they are staged in shared memory and written with one TMA store of
+// whole 128-byte rows (the store map clips the right ghost columns).  Group
+// 0, whose box would also cover the left ghost columns, stores directly.
+// src/cpu/solver_cpu.cpp:247-279 + :474-498
 // ---------------------------------------------------------------------------
 template <class T, int S, int RY, int BW, int STAGES, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB)
-    sweep_y_kernel(const __grid_constant__ CUtensorMap tm, const SweepArgs<T> a) {
+    sweep_y_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tm_out,
+                   const SweepArgs<T> a) {
     constexpr int STAGE = 4 * RY * BW;
-    static_assert(BW >= 32 + kTOff - kSOff, "box too narrow");
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
-    static_assert(STAGE_BYTES % 128 == 0, "stage buffers must stay 128-byte aligned");
+    constexpr int OSTAGE = 4 * RY * 32;          // output box: 4 fields x RY rows x 32 columns
+    constexpr uint32_t OSTAGE_BYTES = OSTAGE * sizeof(T);
+    static_assert(STAGE_BYTES % 128 == 0 && OSTAGE_BYTES % 128 == 0, "stage buffers must stay 128-byte aligned");
+    static_assert(BW >= 32 + kTOff - kSOff, "box too narrow");
+    static_assert(RY == 4, "the 4-row output lag must be exactly one box");
     extern __shared__ __align__(1024) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int task = blockIdx.x * NW + warp;
@@ -404,16 +414,19 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 
     unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
     T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
+    T* obuf = reinterpret_cast<T*>(base + (size_t)NW * STAGES * STAGE_BYTES) + (size_t)warp * 2 * OSTAGE;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * (STAGES * STAGE_BYTES + 2 * OSTAGE_BYTES)) +
+                    warp * STAGES;
 
     const int rs = task / a.nseg;                // row segment
     const int g = task - rs * a.nseg;            // group of 32 S columns
-    const int r0 = rs * a.seg;                   // first interior output row
+    const int r0 = rs * a.seg;                   // first interior output row (a multiple of RY)
     const int e = min(r0 + a.seg, a.ny);
-    const int nst = (e + 4 - r0 + RY - 1) / RY;  // boxes: Utmp rows [r0, e+4)
+    const int nst = 1 + (e - r0 + RY - 1) / RY;  // warm-up box + output boxes
     const int sc = g * 32 + lane;                // S column of this lane
     const int i = sc - kSOff;                    // its interior column
     const bool col_ok = i >= 0 && i < a.nx;
+    const bool direct = g == 0;                  // this group stores without TMA
     const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dy
     const T lam = T(lam_d);
     const T hl = T(0.5 * lam_d);
@@ -422,6 +435,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bar[s]), 1);
         fence_mbar_init();
         tma_prefetch_desc(&tm);
+        tma_prefetch_desc(&tm_out);
     }
     __syncwarp();
     auto issue = [&](int k) {
@@ -439,7 +453,6 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     line.reset();
     T smax = T(0), ssum = T(0);
     const bool edge = col_ok && (i <= 1 || i >= a.nx - 2);   // writes x-ghost columns
-    const long long pitch = a.out.pitch, plane = a.out.plane;
     bool timed_out = false;
     int kfail = nst;
     for (int k = 0; k < nst; ++k) {
@@ -450,20 +463,25 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             break;
         }
         const T* sb = buf + s * STAGE + lane + (kTOff - kSOff);
-        const int ir0 = r0 + k * RY - 4;          // interior row of the first output of this box
-        T* op = a.out.base + (long long)(ir0 + 2) * pitch + sc;
+        T* ob = obuf + (k & 1) * OSTAGE + lane;
+        if (k >= 3 && lane == 0) bulk_wait_read1();   // output buffer k&1 was stored at box k-2
+        __syncwarp();
+        const int ir0 = r0 + (k - 1) * RY;        // interior row of this box's first output
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
             // normal momentum of the y-sweep is rho*v (plane 2)
             const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
             const Cons<T> N = line.push(U, hl, lam);
+            ob[rr * 32] = N.r;
+            ob[(RY + rr) * 32] = N.mt;
+            ob[(2 * RY + rr) * 32] = N.mn;
+            ob[(3 * RY + rr) * 32] = N.e;
             const int ir = ir0 + rr;
-            if (col_ok && ir >= r0 && ir < e) {
-                T* o = op + rr * pitch;
-                o[0] = N.r; o[plane] = N.mt; o[2 * plane] = N.mn; o[3 * plane] = N.e;
+            if (k > 0 && col_ok && ir < e) {
                 const T sp = signal_speed_fast(N);
                 ssum += sp;                       // NaN / inf propagate: checked once at the end
                 smax = Ar<T>::fmax_(smax, sp);
+                if (direct) store_cell(a.out, ir + 2, sc, N, 2, 1, false);
                 if (edge) {                       // x-ghost columns of Unew read by the next x-sweep
                     if (i == 0) {
                         if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
@@ -481,18 +499,23 @@ __global__ void __launch_bounds__(NW * 32, MINB)
                 }
             }
         }
+        fence_proxy_async_smem();
         __syncwarp();
-        if (lane == 0 && k + STAGES < nst) {
-            fence_proxy_async_smem();
-            issue(k + STAGES);
+        if (lane == 0) {
+            if (k > 0 && !direct) {
+                tma_store_3d(&tm_out, smem_u32(obuf + (k & 1) * OSTAGE), g * 32, ir0 + 2, 0);
+                bulk_commit();
+            }
+            if (k + STAGES < nst) issue(k + STAGES);
         }
     }
-    const bool bad = !(Ar<T>::fabs_(ssum) < T(INFINITY));
+    if (lane == 0) bulk_wait0();
     if (timed_out) {
         const int last = min(kfail + STAGES, nst);
         for (int k = kfail + 1; k < last; ++k)
             (void)mbar_wait_bounded(smem_u32(&bar[k % STAGES]), (uint32_t)((k / STAGES) & 1));
     }
+    const bool bad = !(Ar<T>::fabs_(ssum) < T(INFINITY));
     warp_arrive<T>(ctl, smax, bad, timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);
 }
 

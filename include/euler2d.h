@@ -165,6 +165,12 @@ void eu_host_free(void* p);
  * Read-only: "tasks_x", "tasks_y".  Used by the tile-shape autotuner. */
 int eu_set_option(eu_handle* h, const char* name, long long value);
 int eu_get_option(eu_handle* h, const char* name, long long* value);
+/* Diagnostics (no reference counterpart): copy the raw device planes of
+ * state buffer 0/1 (which = 0, 1) or of the x-sweep output (which = 2) to
+ * `out` (4 planes of `plane` elements in the handle's precision; interior
+ * cell (i, j) of a state buffer at column i+6, row j+2; of the x-sweep output
+ * at column i+8).  out == NULL only reports the pitch and plane length. */
+int eu_read_planes(eu_handle* h, int which, void* out, size_t bytes, long long* pitch, long long* plane);
 /* Device used by handles created afterwards on the calling thread. */
 int eu_set_device(int device);
 /* Name of device 0 and its SM count, for logs. */

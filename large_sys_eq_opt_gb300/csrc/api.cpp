@@ -150,6 +150,14 @@ int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long 
     return EU_OK;
 }
 
+// Width of the y-sweep store map: the interior's end (column nx+kSOff)
+// rounded down to 16 bytes, because TMA stores clip at that granularity and
+// must not reach the right ghost columns.
+long long wclip_of(const eu_handle* h) {
+    const long long per16 = 16 / (long long)h->esz;
+    return std::max<long long>((h->cfg.nx + kSOff) / per16 * per16, per16);
+}
+
 int encode_all(eu_handle* h) {
     for (int b = 0; b < 2; ++b)
         if (int rc = encode(h, &h->tm_x[b], h->S[b], h->cfg.nx + kSOff + 2, h->pitch_s, h->plane_s, h->K.box_x, 32,
@@ -161,7 +169,7 @@ int encode_all(eu_handle* h) {
                         CU_TENSOR_MAP_SWIZZLE_32B, 256, h->cfg.ny + 2))
         return rc;
     for (int b = 0; b < 2; ++b)
-        if (int rc = encode(h, &h->tm_yo[b], h->S[b], h->cfg.nx + kSOff, h->pitch_s, h->plane_s, 32, h->K.ry,
+        if (int rc = encode(h, &h->tm_yo[b], h->S[b], wclip_of(h), h->pitch_s, h->plane_s, 32, h->K.ry,
                             CU_TENSOR_MAP_SWIZZLE_NONE, 256))
             return rc;
     return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry,
@@ -231,6 +239,7 @@ template <class T> SweepArgs<T> y_args(const eu_handle* h, int cur) {
     a.bc_hi = h->bc[EU_SIDE_RIGHT];
     a.out_index = 1 - cur;
     a.finalize = 1;
+    a.wclip = (int)wclip_of(h);
     a.d = h->dy;
     return a;
 }
@@ -929,6 +938,20 @@ int eu_get_option(eu_handle* h, const char* name, long long* value) {
     else if (k == "sm_count") *value = h->sm_count;
     else if (k == "tasks_y") *value = h->ntasks_y;
     else return fail(h, EU_ERR_INVALID, "unknown option " + k);
+    return EU_OK;
+}
+
+int eu_read_planes(eu_handle* h, int which, void* out, size_t bytes, long long* pitch, long long* plane) {
+    if (!h || which < 0 || which > 2) return fail(h, EU_ERR_INVALID, "bad argument");
+    void* src = which < 2 ? h->S[which] : h->Tm;
+    const long long pl = which < 2 ? h->plane_s : h->plane_t;
+    if (pitch) *pitch = which < 2 ? h->pitch_s : h->pitch_t;
+    if (plane) *plane = pl;
+    const size_t need = (size_t)(4 * pl) * h->esz;
+    if (!out) return EU_OK;
+    if (bytes < need) return fail(h, EU_ERR_INVALID, "buffer too small");
+    EU_CUDA(h, cudaMemcpyAsync(out, src, need, cudaMemcpyDeviceToHost, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
     return EU_OK;
 }
 

@@ -74,6 +74,8 @@ template <class T> struct SweepArgs {
     int bc_lo, bc_hi;    // x-sweep: bottom/top; y-sweep: left/right (ghost lines it writes)
     int out_index;       // y-sweep: index of the buffer it writes (becomes Ctl::cur)
     int finalize;        // y-sweep: 1 = advance t/step and compute the next dt
+    int wclip;           // y-sweep: S columns >= wclip are stored directly (TMA stores clip at
+                         // 16-byte granularity, so the store map ends on a 16-byte boundary)
     double d;            // dx (x-sweep) or dy (y-sweep); the step uses dt/d
     T* snap;             // x-sweep: snapshot storage, interior SoA [k][f][ny][nx]
     long long snap_plane, snap_stride;

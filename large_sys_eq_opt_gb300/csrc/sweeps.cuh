@@ -390,8 +390,10 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 // a cell is final four rows after it enters, so box k >= 1 yields the output
 // rows [r0 + 4(k-1), r0 + 4k) of this segment (box 0 only warms the window
 // up); they are staged in shared memory and written with one TMA store of
-// whole 128-byte rows (the store map clips the right ghost columns).  Group
-// 0, whose box would also cover the left ghost columns, stores directly.
+// whole 128-byte rows.  The store map ends at the last 16-byte boundary
+// before the right ghost columns (TMA stores clip at 16-byte granularity);
+// columns past it, and group 0 whose box would also cover the left ghost
+// columns, are stored directly.
 // src/cpu/solver_cpu.cpp:247-279 + :474-498
 // ---------------------------------------------------------------------------
 template <class T, int S, int RY, int BW, int STAGES, int NW, int MINB>
@@ -426,7 +428,9 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     const int sc = g * 32 + lane;                // S column of this lane
     const int i = sc - kSOff;                    // its interior column
     const bool col_ok = i >= 0 && i < a.nx;
-    const bool direct = g == 0;                  // this group stores without TMA
+    // Lanes that store without TMA: all of group 0 (its box would cover the
+    // left ghost columns) and the columns past the store map's 16-byte end.
+    const bool direct = g == 0 || sc >= a.wclip;
     const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dy
     const T lam = T(lam_d);
     const T hl = T(0.5 * lam_d);
@@ -502,7 +506,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) {
-            if (k > 0 && !direct) {
+            if (k > 0 && g != 0 && g * 32 < a.wclip) {
                 tma_store_3d(&tm_out, smem_u32(obuf + (k & 1) * OSTAGE), g * 32, ir0 + 2, 0);
                 bulk_commit();
             }

@@ -52,7 +52,7 @@ EXPORTS = (
     "eu_download_aos", "eu_compute_dt", "eu_advance", "eu_step_n", "eu_run", "eu_get_time",
     "eu_totals", "eu_compute_dt_host", "eu_advance_host", "eu_step_host", "eu_time_steps",
     "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
-    "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option",
+    "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option", "eu_read_planes",
 )
 
 _lib = None
@@ -107,6 +107,8 @@ def load(path: str = LIB_PATH):
     L.eu_set_device.argtypes = [C.c_int]
     L.eu_set_option.argtypes = [H, C.c_char_p, C.c_longlong]
     L.eu_get_option.argtypes = [H, C.c_char_p, C.POINTER(C.c_longlong)]
+    L.eu_read_planes.argtypes = [H, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_longlong),
+                                 C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -251,6 +253,18 @@ class Solver:
         v = C.c_longlong()
         self._check(self._L.eu_get_option(self._h, name.encode(), C.byref(v)))
         return v.value
+
+    def read_planes(self, which: int) -> np.ndarray:
+        """Raw device planes (diagnostics): array [4, rows, pitch] of the
+        handle's precision; state buffers hold interior (i, j) at [.., j+2, i+6],
+        the x-sweep output at [.., j+2, i+8]."""
+        pitch, plane = C.c_longlong(), C.c_longlong()
+        self._check(self._L.eu_read_planes(self._h, int(which), None, 0, C.byref(pitch), C.byref(plane)))
+        dt = np.float32 if self.precision in ("fp32", FP32) else np.float64
+        out = np.empty(4 * plane.value, dtype=dt)
+        self._check(self._L.eu_read_planes(self._h, int(which), out.ctypes.data_as(C.c_void_p), out.nbytes, None, None))
+        rows = self.cfg.ny + 4
+        return out.reshape(4, plane.value)[:, :rows * pitch.value].reshape(4, rows, pitch.value)
 
     def totals(self) -> np.ndarray:
         out = np.zeros(4)

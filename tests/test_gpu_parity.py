@@ -187,3 +187,53 @@ def test_nonphysical_state_is_reported(E):
         with pytest.raises(E.EulerError) as ei:
             s.compute_dt(0.8)
         assert ei.value.code == 4
+
+
+@pytest.mark.parametrize("prec", ("fp32", "fp64"))
+@pytest.mark.parametrize("nx", (37, 256, 257, 258, 259))
+def test_device_ghost_lines_after_a_step(E, prec, nx):
+    """After one device step the y-sweep must leave the x-ghost columns of the
+    new state equal to the boundary rule applied to its interior (the next
+    x-sweep reads them), and the x-sweep must leave Utmp's y-ghost rows equal
+    to the rule applied to its interior (the y-sweep reads them)."""
+    from large_sys_eq_opt_gb300.cases import CaseConfig
+    ny = 45
+    for bc in ((0, 0, 0, 0), (1, 1, 1, 1)):
+        cfg = CaseConfig(nx, ny, 2, 0.0, 1.0, 0.0, 1.0, 0.8, 0.25)
+        with E.Solver(cfg, prec, "hllc", bc=bc) as s:
+            s._check(s._L.eu_init_blast(s._h, 0.3, 0.4, 0.2, 1.0, 2.0, 0.2, 0.3))
+            s.apply_boundary()
+            s.advance(s.compute_dt(0.8))
+            S = s.read_planes(1)
+            rows = slice(2, ny + 2)
+            i0, iN = 6, nx + 5                     # S columns of interior 0 and nx-1
+            for g, src in ((5, i0), (4, i0 if bc[0] == 0 else i0 + 1)):
+                sign = np.array([1, -1 if bc[0] else 1, 1, 1])[:, None]
+                assert np.array_equal(S[:, rows, g], sign * S[:, rows, src]), (prec, nx, bc, g)
+            for g, src in ((nx + 6, iN), (nx + 7, iN if bc[1] == 0 else iN - 1)):
+                sign = np.array([1, -1 if bc[1] else 1, 1, 1])[:, None]
+                assert np.array_equal(S[:, rows, g], sign * S[:, rows, src]), (prec, nx, bc, g)
+            Tm = s.read_planes(2)
+            cols = slice(8, nx + 8)
+            for r, src in ((1, 2), (0, 2 if bc[2] == 0 else 3)):
+                sign = np.array([1, 1, -1 if bc[2] else 1, 1])[:, None]
+                assert np.array_equal(Tm[:, r, cols], sign * Tm[:, src, cols]), (prec, nx, bc, r)
+            for r, src in ((ny + 2, ny + 1), (ny + 3, ny + 1 if bc[3] == 0 else ny)):
+                sign = np.array([1, 1, -1 if bc[3] else 1, 1])[:, None]
+                assert np.array_equal(Tm[:, r, cols], sign * Tm[:, src, cols]), (prec, nx, bc, r)
+
+
+@pytest.mark.parametrize("nx,ny", ((257, 131), (130, 67)))
+def test_fp32_device_run_tracks_fp64_oracle(E, port, nx, ny):
+    """FP32 device-resident run (fused dt, graphs, ghost lines written by the
+    sweeps) against the FP64 oracle on odd sizes."""
+    g = Grid(nx, ny, 0.0, 2.0, 0.0, 1.0)
+    U = port.init_blast(g, cx=1.0, cy=0.5, r=0.3)
+    port.run(U, g, 0.8, 0.1, "hllc")
+    with E.Solver(cfg_of(g, 0.8, 0.1), "fp32", "hllc") as s:
+        s._check(s._L.eu_init_blast(s._h, 1.0, 0.5, 0.3, 1.0, 1.0, 0.125, 0.1))
+        info = s.run(0.1)
+        got = s.download()
+    assert info["status"] == 0
+    e = l1(interior(got)[..., 0], interior(U)[..., 0])
+    assert e <= 1e-5, e

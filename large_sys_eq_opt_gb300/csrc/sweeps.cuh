@@ -457,6 +457,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     line.reset();
     T smax = T(0), ssum = T(0);
     const bool edge = col_ok && (i <= 1 || i >= a.nx - 2);   // writes x-ghost columns
+    const bool special = __any_sync(0xffffffffu, direct || edge);
     bool timed_out = false;
     int kfail = nst;
     for (int k = 0; k < nst; ++k) {
@@ -471,6 +472,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         if (k >= 3 && lane == 0) bulk_wait_read1();   // output buffer k&1 was stored at box k-2
         __syncwarp();
         const int ir0 = r0 + (k - 1) * RY;        // interior row of this box's first output
+        const bool rows_ok = k > 0 && ir0 + RY <= e;   // every row of the box is an output row
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
             // normal momentum of the y-sweep is rho*v (plane 2)
@@ -481,12 +483,15 @@ __global__ void __launch_bounds__(NW * 32, MINB)
             ob[(2 * RY + rr) * 32] = N.mn;
             ob[(3 * RY + rr) * 32] = N.e;
             const int ir = ir0 + rr;
-            if (k > 0 && col_ok && ir < e) {
-                const T sp = signal_speed_fast(N);
+            const bool out_ok = col_ok && (rows_ok || (k > 0 && ir < e));
+            const T sp = signal_speed_fast(N);
+            if (out_ok) {
                 ssum += sp;                       // NaN / inf propagate: checked once at the end
                 smax = Ar<T>::fmax_(smax, sp);
-                if (direct) store_cell(a.out, ir + 2, sc, N, 2, 1, false);
-                if (edge) {                       // x-ghost columns of Unew read by the next x-sweep
+            }
+            if (special) {                        // warp-uniform: few warps store anything directly
+                if (out_ok && direct) store_cell(a.out, ir + 2, sc, N, 2, 1, false);
+                if (out_ok && edge) {             // x-ghost columns of Unew read by the next x-sweep
                     if (i == 0) {
                         if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
                         else { store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, false);

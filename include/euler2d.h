@@ -118,6 +118,11 @@ int eu_compute_dt(eu_handle* h, double cfl, double* dt);
 /* advance_second_order (src/cpu/solver_cpu.cpp:400-499) on the device state:
  * x-sweep, BC, y-sweep, BC, with the given dt. */
 int eu_advance(eu_handle* h, double dt);
+/* advance_first_order (src/cpu/solver_cpu.cpp:315-369): first-order
+ * Godunov step with the handle's Riemann solver, ghosts of the result
+ * refilled by the boundary rule. */
+int eu_advance_first_order(eu_handle* h, double dt);
+int eu_advance_first_order_host(eu_handle* h, const double* Uold, double* Unew, double dt);
 /* n steps device-resident in a CUDA graph.  dts == NULL: each dt from the
  * fused CFL reduction (no t_end clip); otherwise the frozen list dts[0..n). */
 int eu_step_n(eu_handle* h, long long n, const double* dts);

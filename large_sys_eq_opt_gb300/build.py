@@ -21,6 +21,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libeuler2d.so")
+CLI = os.path.join(PKG, "bin", "euler2d_gb300")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -49,7 +50,7 @@ def units():
 
 def _sources_digest() -> str:
     h = hashlib.sha256()
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, os.path.join(PKG, "cli")):
         for fn in sorted(os.listdir(d)):
             p = os.path.join(d, fn)
             if os.path.isfile(p):
@@ -66,7 +67,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     os.makedirs(BUILD, exist_ok=True)
     stamp = os.path.join(BUILD, "stamp")
     digest = _sources_digest()
-    if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == digest:
+    if (not force and os.path.exists(LIB) and os.path.exists(CLI) and os.path.exists(stamp)
+            and open(stamp).read() == digest):
         return LIB
     cc = nvcc()
     jobs = []
@@ -93,6 +95,15 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + " ".join(link) + "\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
+    # the C++ command-line driver (links the library through an $ORIGIN rpath)
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    cxx = shutil.which("g++") or "g++"
+    cli = [cxx, "-O2", "-std=c++17", "-I" + INCLUDE, os.path.join(PKG, "cli", "euler2d_gb300.cpp"),
+           "-o", CLI + ".tmp", "-L" + PKG, "-leuler2d", "-Wl,-rpath,$ORIGIN/..", "-lpthread"]
+    r = subprocess.run(cli, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n" + " ".join(cli) + "\n" + r.stdout + r.stderr)
+    os.replace(CLI + ".tmp", CLI)
     with open(stamp, "w") as f:
         f.write(digest)
     return LIB

@@ -629,6 +629,37 @@ int eu_advance(eu_handle* h, double dt) {
     return h->hctl->status & kStatusTimeout ? status_code(h) : EU_OK;
 }
 
+int eu_advance_first_order(eu_handle* h, double dt) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (!(dt >= 0.0) || !std::isfinite(dt)) return fail(h, EU_ERR_INVALID, "dt must be finite and >= 0");
+    const int nxt = 1 - h->cur;
+    if (h->prec == EU_FP32) {
+        const Planes<float> a = planes_s<float>(h, h->cur), b = planes_s<float>(h, nxt);
+        EU_CUDA(h, h->K.first(&a, &b, h->cfg.nx, h->cfg.ny, dt / h->dx, dt / h->dy, h->st));
+    } else {
+        const Planes<double> a = planes_s<double>(h, h->cur), b = planes_s<double>(h, nxt);
+        EU_CUDA(h, h->K.first(&a, &b, h->cfg.nx, h->cfg.ny, dt / h->dx, dt / h->dy, h->st));
+    }
+    EU_CUDA(h, fill_ghosts(h, nxt));  // src/cpu/solver_cpu.cpp:368
+    Ctl& c = *h->hctl;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    h->cur = nxt;
+    c.cur = nxt;
+    c.t += dt;
+    c.step += 1;
+    return ctl_push(h);
+}
+
+int eu_advance_first_order_host(eu_handle* h, const double* Uold, double* Unew, double dt) {
+    if (!h || !Uold || !Unew) return fail(h, EU_ERR_INVALID, "null argument");
+    int rc = upload_to(h, h->cur, Uold);
+    if (rc) return rc;
+    if ((rc = eu_advance_first_order(h, dt))) return rc;
+    if ((rc = download_from_state(h, h->cur, Unew))) return rc;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
 int eu_step_n(eu_handle* h, long long n, const double* dts) {
     if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
     if (n < 0) return fail(h, EU_ERR_INVALID, "n must be >= 0");

@@ -85,8 +85,12 @@ template <class T> struct SweepArgs {
 using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args,
                                     int ctas, cudaStream_t s);
 
+using FirstOrderLaunch = cudaError_t (*)(const void* in, const void* out, int nx, int ny, double dtdx,
+                                         double dtdy, cudaStream_t s);
+
 struct SweepKernels {
     SweepLaunch x, y;
+    FirstOrderLaunch first;  // first-order Godunov step (in/out: Planes<T>*)
     int (*occ_x)();      // resident CTAs per SM of each kernel
     int (*occ_y)();
     int box_x;           // x-sweep box: box_x columns (32 bytes) x 32 rows, 32-byte swizzle

@@ -17,6 +17,7 @@
 #define LAUNCH_X EU_NAME(launch_x, EU_PREC, EU_SOLVER)
 #define LAUNCH_Y EU_NAME(launch_y, EU_PREC, EU_SOLVER)
 #define OCC_X EU_NAME(occ_x, EU_PREC, EU_SOLVER)
+#define LAUNCH_F EU_NAME(launch_first, EU_PREC, EU_SOLVER)
 #define OCC_Y EU_NAME(occ_y, EU_PREC, EU_SOLVER)
 
 namespace eu {
@@ -64,6 +65,15 @@ static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap* tm_out, co
     return cudaGetLastError();
 }
 
+static cudaError_t LAUNCH_F(const void* in, const void* out, int nx, int ny, double dtdx, double dtdy,
+                            cudaStream_t s) {
+    long long blocks = ((long long)nx * ny + 255) / 256;
+    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    first_order_kernel<T, SOL><<<(int)blocks, 256, 0, s>>>(*static_cast<const Planes<T>*>(in),
+                                                           *static_cast<const Planes<T>*>(out), nx, ny, dtdx, dtdy);
+    return cudaGetLastError();
+}
+
 static int OCC_X() {
     auto k = sweep_x_kernel<T, SOL, SX, NW, MINB_X>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX);
@@ -87,6 +97,7 @@ SweepKernels EU_NAME(sweep_kernels, EU_PREC, EU_SOLVER)() {
     k.x = LAUNCH_X;
     k.y = LAUNCH_Y;
     k.occ_x = OCC_X;
+    k.first = LAUNCH_F;
     k.occ_y = OCC_Y;
     k.box_x = CX;
     k.ry = RY;

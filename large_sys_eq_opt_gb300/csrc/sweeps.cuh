@@ -528,4 +528,39 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     warp_arrive<T>(ctl, smax, bad, timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);
 }
 
+// ---------------------------------------------------------------------------
+// First-order Godunov step (src/cpu/solver_cpu.cpp:315-369): four interface
+// fluxes per cell from the unreconstructed neighbours, one thread per cell,
+// ghosts of the input read as given; the caller refills the output's ghost
+// frame afterwards (the reference ends with apply_transmissive_boundary).
+// ---------------------------------------------------------------------------
+template <class T, int S>
+__global__ void __launch_bounds__(256) first_order_kernel(Planes<T> in, Planes<T> out, int nx, int ny,
+                                                          double dtdx, double dtdy) {
+    const long long total = (long long)nx * ny;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / nx), i = (int)(idx - (long long)j * nx);
+        const T* c = in.base + (long long)(j + 2) * in.pitch + (i + kSOff);
+        auto ld = [&](long long off) {
+            const T* q = c + off;
+            return Cons<T>{q[0], q[in.plane], q[2 * in.plane], q[3 * in.plane]};
+        };
+        const Cons<T> U = ld(0), W = ld(-1), E_ = ld(1), Sd = ld(-in.pitch), Nd = ld(in.pitch);
+        // x faces in (n, t) = (rho u, rho v); y faces in (n, t) = (rho v, rho u)
+        auto swp = [](const Cons<T>& a) { return Cons<T>{a.r, a.mt, a.mn, a.e}; };
+        const Cons<T> Fxp = riemann<S>(U, cons_to_prim(U), E_, cons_to_prim(E_));
+        const Cons<T> Fxm = riemann<S>(W, cons_to_prim(W), U, cons_to_prim(U));
+        const Cons<T> Uy = swp(U), Ny = swp(Nd), Sy = swp(Sd);
+        const Cons<T> Gp = riemann<S>(Uy, cons_to_prim(Uy), Ny, cons_to_prim(Ny));
+        const Cons<T> Gm = riemann<S>(Sy, cons_to_prim(Sy), Uy, cons_to_prim(Uy));
+        const T ax = T(dtdx), ay = T(dtdy);
+        T* o = out.base + (long long)(j + 2) * out.pitch + (i + kSOff);
+        o[0] = (U.r - ax * (Fxp.r - Fxm.r)) - ay * (Gp.r - Gm.r);
+        o[out.plane] = (U.mn - ax * (Fxp.mn - Fxm.mn)) - ay * (Gp.mt - Gm.mt);
+        o[2 * out.plane] = (U.mt - ax * (Fxp.mt - Fxm.mt)) - ay * (Gp.mn - Gm.mn);
+        o[3 * out.plane] = (U.e - ax * (Fxp.e - Fxm.e)) - ay * (Gp.e - Gm.e);
+    }
+}
+
 }  // namespace eu

@@ -53,6 +53,7 @@ EXPORTS = (
     "eu_totals", "eu_compute_dt_host", "eu_advance_host", "eu_step_host", "eu_time_steps",
     "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
     "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option", "eu_read_planes",
+    "eu_advance_first_order", "eu_advance_first_order_host",
 )
 
 _lib = None
@@ -109,6 +110,8 @@ def load(path: str = LIB_PATH):
     L.eu_get_option.argtypes = [H, C.c_char_p, C.POINTER(C.c_longlong)]
     L.eu_read_planes.argtypes = [H, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_longlong),
                                  C.POINTER(C.c_longlong)]
+    L.eu_advance_first_order.argtypes = [H, C.c_double]
+    L.eu_advance_first_order_host.argtypes = [H, _dp, _dp, C.c_double]
     _lib = L
     return L
 
@@ -286,6 +289,15 @@ class Solver:
 
     def advance(self, dt: float):
         self._check(self._L.eu_advance(self._h, float(dt)))
+
+    def advance_first_order(self, dt: float):
+        self._check(self._L.eu_advance_first_order(self._h, float(dt)))
+
+    def advance_first_order_host(self, Uold: np.ndarray, dt: float) -> np.ndarray:
+        Uold = np.ascontiguousarray(Uold, dtype=np.float64)
+        Unew = np.empty(self.shape)
+        self._check(self._L.eu_advance_first_order_host(self._h, _p(Uold), _p(Unew), float(dt)))
+        return Unew
 
     def step_n(self, n: int, dts=None):
         if dts is None:

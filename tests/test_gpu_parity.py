@@ -80,7 +80,9 @@ def test_single_step_golden_cases(E, golden_dir, solver):
         dt = float(d[f"{name}/dt"][0])
         with E.Solver(cfg_of(g), "fp64", solver) as s:
             Utmp, Unew = s.advance_host(U, dt)
-        for lbl, got, ref in (("Utmp", Utmp, d[f"{name}/{solver}/Utmp"]), ("Unew", Unew, d[f"{name}/{solver}/Unew"])):
+            U1 = s.advance_first_order_host(U, dt)
+        for lbl, got, ref in (("Utmp", Utmp, d[f"{name}/{solver}/Utmp"]), ("Unew", Unew, d[f"{name}/{solver}/Unew"]),
+                              ("U1", U1, d[f"{name}/{solver}/U1"])):
             scale = np.maximum(np.abs(ref), 1.0)
             err = float(np.max(np.abs(got - ref) / scale))
             assert err <= 1e-12, (name, solver, lbl, err)

@@ -141,6 +141,29 @@ int eu_set_dt_log(eu_handle* h, long long capacity);
 int eu_get_dt_log(eu_handle* h, double* out, long long n);
 /* FP64 totals of rho, rhou, rhov, E over the interior (conserved audit). */
 int eu_totals(eu_handle* h, double out[4]);
+/* eu_totals for callers that cannot let this library allocate device memory
+ * (no counterpart in the reference).  For a caller that owns all device
+ * memory through its own pool -- a framework's caching allocator, or an
+ * application that reserves the HBM at start-up -- and so cannot create a
+ * handle (eu_create allocates); cudaMalloc/cudaFree would synchronise the
+ * device and fragment that pool.  Allocates nothing: no cudaMalloc/cudaFree,
+ * no allocating library.
+ *   d_aos   the caller's grid in device memory of the current device, Grid2D
+ *           AoS layout with ghosts ((nx+4)*(ny+4)*4 doubles), 16-byte aligned;
+ *           only interior cells are read.
+ *   d_out   4 doubles of the caller's device memory (8-byte aligned) that
+ *           receive the totals; they need not start at zero.
+ *   stream  cudaStream_t to enqueue on (NULL = the default stream).  The call
+ *           returns once the work is enqueued; d_out is ready when the stream
+ *           reaches it.
+ * Scratch: a fixed 1 MiB array inside the library (8 doubles per interior
+ * row).  ny > 16384 is rejected with EU_ERR_INVALID; nothing in the scratch
+ * has to start at zero.  The first call on each device (with that device
+ * current) looks the scratch up with cudaGetSymbolAddress: make it before any
+ * stream capture begins.  All calls on one device share the scratch, so two
+ * calls whose work overlaps (different streams or host threads, unordered)
+ * race and give wrong totals: order them on one stream or with events. */
+int eu_totals_noalloc(const double* d_aos, int nx, int ny, double* d_out, void* stream);
 
 /* ---- drop-in calls on host grids (what the reference's callers pass) ------- */
 /* compute_dt(const Grid2D&, double): upload, reduce, read back dt. */

@@ -44,6 +44,7 @@ def units():
                 flags.append("--use_fast_math")
             out.append((os.path.join(CSRC, "kern_sweeps.cu"), f"kern_{prec}_{solver}.o", flags))
     out.append((os.path.join(CSRC, "aux_kernels.cu"), "aux_kernels.o", []))
+    out.append((os.path.join(CSRC, "noalloc.cu"), "noalloc.o", []))
     out.append((os.path.join(CSRC, "api.cpp"), "api.o", ["-x", "cu"]))
     return out
 

@@ -395,6 +395,11 @@ int download_from_state(eu_handle* h, int b, double* aos) {
 
 }  // namespace
 
+namespace eu {
+// Message for eu_last_error(NULL), for entry points defined in other units.
+void set_global_error(const char* msg) { g_err = msg; }
+}  // namespace eu
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

@@ -53,7 +53,7 @@ EXPORTS = (
     "eu_totals", "eu_compute_dt_host", "eu_advance_host", "eu_step_host", "eu_time_steps",
     "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
     "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option", "eu_read_planes",
-    "eu_advance_first_order", "eu_advance_first_order_host",
+    "eu_advance_first_order", "eu_advance_first_order_host", "eu_totals_noalloc",
 )
 
 _lib = None
@@ -112,6 +112,7 @@ def load(path: str = LIB_PATH):
                                  C.POINTER(C.c_longlong)]
     L.eu_advance_first_order.argtypes = [H, C.c_double]
     L.eu_advance_first_order_host.argtypes = [H, _dp, _dp, C.c_double]
+    L.eu_totals_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 

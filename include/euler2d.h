@@ -165,6 +165,27 @@ int eu_totals(eu_handle* h, double out[4]);
  * race and give wrong totals: order them on one stream or with events. */
 int eu_totals_noalloc(const double* d_aos, int nx, int ny, double* d_out, void* stream);
 
+/* ---- discrete adjoint (no counterpart in the reference) ---------------------- */
+/* Gradient of a scalar objective J(U_N) of the state after nsteps steps with
+ * the frozen step sizes dts[0..nsteps), with respect to the current state
+ * U_0, through the discrete adjoint of the split step (transposed
+ * reconstruction with minmod subgradients, transposed Riemann-flux
+ * Jacobians, the exact solver through implicit differentiation at the
+ * converged p*, transposed boundary rule).
+ * eu_adjoint_forward runs the nsteps steps from the current state, keeping a
+ * checkpoint every ckpt_k steps (plus the last segment's intermediate
+ * states); the handle's state becomes U_N and its time advances by sum(dts).
+ * eu_adjoint_backward takes dJ/dU_N and returns dJ/dU_0 (both host grids in
+ * Grid2D AoS layout; ghost entries of the input are ignored, those of the
+ * output are zero), recomputing each earlier segment's states from its
+ * checkpoint.  It can be called repeatedly after one forward pass.  The
+ * arithmetic is the handle's precision.  Needs nx, ny >= 2. */
+int eu_adjoint_forward(eu_handle* h, long long nsteps, const double* dts, int ckpt_k);
+int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0);
+/* Device time (CUDA events) of the last eu_adjoint_forward (ms[0], its steps
+ * only) and eu_adjoint_backward (ms[1], recomputation + adjoint sweeps). */
+int eu_adjoint_timing(eu_handle* h, float ms[2]);
+
 /* ---- drop-in calls on host grids (what the reference's callers pass) ------- */
 /* compute_dt(const Grid2D&, double): upload, reduce, read back dt. */
 int eu_compute_dt_host(eu_handle* h, const double* U, double cfl, double* dt);

@@ -1,8 +1,9 @@
 """Build the in-tree CUDA library (libeuler2d.so) for sm_103a.
 
-Ten translation units compile in parallel with nvcc (one -gencode, no
-cmake): the sweep kernels once per (precision, Riemann solver), the auxiliary
-kernels and the host runtime.  The FP32 units use fast approximate
+The translation units compile in parallel with nvcc (one -gencode, no
+cmake): the sweep kernels and the adjoint sweep kernels once per (precision,
+Riemann solver), the auxiliary kernels, the allocation-free audit and the
+host runtime.  The FP32 units use fast approximate
 reciprocal/square root (--use_fast_math); the FP64 units use IEEE division
 and square root.  Objects go to large_sys_eq_opt_gb300/_build/, the library
 to large_sys_eq_opt_gb300/libeuler2d.so.
@@ -43,6 +44,12 @@ def units():
             if prec == 32:
                 flags.append("--use_fast_math")
             out.append((os.path.join(CSRC, "kern_sweeps.cu"), f"kern_{prec}_{solver}.o", flags))
+    for prec in (32, 64):
+        for solver in range(4):
+            flags = [f"-DEU_PREC={prec}", f"-DEU_SOLVER={solver}"]
+            if prec == 32:
+                flags.append("--use_fast_math")
+            out.append((os.path.join(CSRC, "adjoint_kernels.cu"), f"adj_{prec}_{solver}.o", flags))
     out.append((os.path.join(CSRC, "aux_kernels.cu"), "aux_kernels.o", []))
     out.append((os.path.join(CSRC, "noalloc.cu"), "noalloc.o", []))
     out.append((os.path.join(CSRC, "api.cpp"), "api.o", ["-x", "cu"]))

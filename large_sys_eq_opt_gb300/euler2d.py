@@ -54,6 +54,7 @@ EXPORTS = (
     "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
     "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option", "eu_read_planes",
     "eu_advance_first_order", "eu_advance_first_order_host", "eu_totals_noalloc",
+    "eu_adjoint_forward", "eu_adjoint_backward", "eu_adjoint_timing",
 )
 
 _lib = None
@@ -113,6 +114,9 @@ def load(path: str = LIB_PATH):
     L.eu_advance_first_order.argtypes = [H, C.c_double]
     L.eu_advance_first_order_host.argtypes = [H, _dp, _dp, C.c_double]
     L.eu_totals_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    L.eu_adjoint_forward.argtypes = [H, C.c_longlong, _dp, C.c_int]
+    L.eu_adjoint_backward.argtypes = [H, _dp, _dp]
+    L.eu_adjoint_timing.argtypes = [H, C.POINTER(C.c_float)]
     _lib = L
     return L
 
@@ -274,6 +278,26 @@ class Solver:
         out = np.zeros(4)
         self._check(self._L.eu_totals(self._h, _p(out)))
         return out
+
+    # -- discrete adjoint ----------------------------------------------------------
+    def adjoint_forward(self, dts, ckpt_k: int = 32):
+        """Run len(dts) frozen-dt steps from the current state, keeping
+        checkpoints every ckpt_k steps for adjoint_backward."""
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        self._check(self._L.eu_adjoint_forward(self._h, len(d), _p(d), int(ckpt_k)))
+
+    def adjoint_backward(self, dJ_dUN: np.ndarray) -> np.ndarray:
+        """dJ/dU_0 for dJ/dU_N (both (ny+4, nx+4, 4) float64; ghosts zero)."""
+        g = np.ascontiguousarray(dJ_dUN, dtype=np.float64)
+        assert g.shape == self.shape
+        out = np.zeros(self.shape)
+        self._check(self._L.eu_adjoint_backward(self._h, _p(g), _p(out)))
+        return out
+
+    def adjoint_timing(self):
+        ms = (C.c_float * 2)()
+        self._check(self._L.eu_adjoint_timing(self._h, ms))
+        return float(ms[0]), float(ms[1])
 
     def time(self):
         t = C.c_double()

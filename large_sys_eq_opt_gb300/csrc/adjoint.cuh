@@ -525,6 +525,13 @@ EUA_HD_NOINLINE bool exact_star_d(double rL, double uL, double pL, double aL, do
     us = 0.5 * (uL + uR + r.f - l.f);
     return fabs(us) < INFINITY;
 }
+// p*, u* in the working type.  (A number type that carries derivatives can
+// overload this to attach dp*/dtheta by implicit differentiation.)
+template <class T>
+EUA_HD void star_refine(const Side<T>&, const Side<T>&, double ps, double us, T& tps, T& tus) {
+    tps = T(ps);
+    tus = T(us);
+}
 template <class T> struct Exact {
     int mode;     // 0..3 HLL kinds (fallbacks), 4 sampled state
     bool left;
@@ -544,8 +551,7 @@ template <class T> EUA_HD Exact<T> exact_plan(const Side<T>& L, const Side<T>& R
         x.mode = hll_kind(L, R, x.sp);
         return x;
     }
-    x.ps = T(ps);
-    x.us = T(us);
+    star_refine(L, R, ps, us, x.ps, x.us);
     x.left = us >= 0.0;
     const Side<T>& K = x.left ? L : R;
     const T sg = x.left ? T(1) : T(-1);

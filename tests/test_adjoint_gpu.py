@@ -1,27 +1,54 @@
-"""Discrete adjoint on the GPU (eu_adjoint_forward / eu_adjoint_backward)
-against central finite differences of the FP64 forward with the same frozen
-dt sequence, an FP64 build of the same adjoint, and the torch.autograd
-wrapper.
+"""Discrete adjoint on the GPU (eu_adjoint_forward / eu_adjoint_backward).
 
 Objective (the adjoint benchmark's): J = sum of rho^2 over the cells whose
 centre lies at radius 0.6 <= r <= 0.8 from (1, 1), at the final step; the
 gradient is taken with respect to the initial rho and p fields (E =
-p/(gamma-1) at u = v = 0).
+p/(gamma-1) at u = v = 0).  Initial state: the blast of [0,2]^2 (rho 1, p 1
+inside radius 0.4, rho 0.125, p 0.1 outside), optionally times a smooth
+perturbation.
 
-The initial state is the blast of [0,2]^2 (rho 1, p 1 inside radius 0.4,
-rho 0.125, p 0.1 outside) plus a smooth perturbation of relative amplitude
-1e-3.  Without it the ambient region is exactly uniform, every limiter
-argument there is exactly zero, and minmod's one-sided response to a
-perturbation (minmod(eps a, eps b) = eps minmod(a, b)) is not linear in the
-direction -- no gradient reproduces it, so finite differences of the exact
-piecewise-constant blast disagree with any adjoint there.
+Checks:
+  * exactness: the FP64 GPU adjoint's directional derivatives against a
+    forward-mode (dual-number) derivative of the same discrete step computed
+    on the CPU (tests/adjoint/adj_check.cpp, file mode) -- same branch
+    decisions, no truncation error;
+  * central finite differences of the FP64 forward (eps 1e-6, the frozen dt
+    sequence) along seeded Gaussian directions.  Minmod is only piecewise
+    linear: every limiter argument that crosses zero (or |a| = |b|) within
+    the eps-perturbation adds an O(eps) error to the difference quotient,
+    and on the exactly piecewise-constant blast every ambient cell sits on
+    such a kink (minmod(eps a, eps b) = eps minmod(a, b) is not linear in the
+    direction).  The difference quotients are therefore compared on the
+    smoothly perturbed blast with a tolerance that reflects the kinks, and
+    their error is shown to shrink with eps;
+  * the FP32 adjoint of the FP32 forward against the FP64 adjoint;
+  * checkpoint recomputation is bit-reproducible; the checkpointed forward
+    equals eu_step_n; the torch.autograd wrapper returns the adjoint.
 """
+import os
+import shutil
+import subprocess
+
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 GAMMA = 1.4
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available for the forward-mode reference")
+    exe = tmp_path_factory.mktemp("adj") / "adj_check"
+    r = subprocess.run([cxx, "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "large_sys_eq_opt_gb300", "csrc"),
+                        os.path.join(ROOT, "tests", "adjoint", "adj_check.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(exe)
 
 
 @pytest.fixture(scope="module")
@@ -46,6 +73,7 @@ def centres(cfg):
 
 
 def blast_fields(cfg, smooth=1e-3):
+    """Blast rho, p times (w, 2 - w) with w = 1 + smooth * (smooth waves)."""
     X, Y = centres(cfg)
     inside = (X - 1.0) ** 2 + (Y - 1.0) ** 2 <= 0.4 ** 2
     rho = np.where(inside, 1.0, 0.125)
@@ -101,12 +129,12 @@ def directions(cfg, count, seed=12345):
     return out
 
 
-def fd_check(E, cfg, solver, nsteps, k, ndir, bc=None, eps=1e-6):
-    rho, p = blast_fields(cfg)
+def fd_check(E, cfg, solver, nsteps, k, ndir, bc=None, eps=1e-6, smooth=1e-3):
+    rho, p = blast_fields(cfg, smooth)
     U0 = grid_of(cfg, rho, p)
     dts = cfl_dts(E, cfg, U0, solver, nsteps)
     mask = ring(cfg)
-    with E.Solver(cfg, "fp64", solver, bc=bc) as s:
+    with E.Solver(cfg, "fp64", solver, bc=bc or (0, 0, 0, 0)) as s:
         s.upload(U0)
         s.adjoint_forward(dts, k)
         UN = s.download()
@@ -121,16 +149,65 @@ def fd_check(E, cfg, solver, nsteps, k, ndir, bc=None, eps=1e-6):
     return errs, g
 
 
+def forward_mode(harness, tmp, cfg, solver_id, dts, rho, p, mask, dirs, bc):
+    """Directional derivatives of J by the CPU forward-mode reference."""
+    fin, fout = tmp / "problem.bin", tmp / "result.bin"
+    hdr = np.array([cfg.nx, cfg.ny, solver_id, len(dts), *bc, len(dirs)], dtype=np.int32)
+    with open(fin, "wb") as f:
+        f.write(hdr.tobytes())
+        f.write(np.array([2.0 / cfg.nx, 2.0 / cfg.ny]).tobytes())
+        for a in (np.asarray(dts), rho, p, mask.astype(np.float64)):
+            f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+        for d in dirs:
+            f.write(np.ascontiguousarray(d, dtype=np.float64).tobytes())
+    r = subprocess.run([harness, str(fin), str(fout)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = np.fromfile(fout, dtype=np.float64)
+    return out[:len(dirs)], out[len(dirs):]
+
+
+def adjoint_dirs(g, dirs):
+    return np.array([np.sum(g[2:-2, 2:-2, 0] * d[0]) + np.sum(g[2:-2, 2:-2, 3] * d[1]) / (GAMMA - 1.0)
+                     for d in dirs])
+
+
+SOLVER_ID = {"hll": 0, "hllc": 1, "exact": 2, "force": 3}
+
+
+@pytest.mark.parametrize("solver,smooth,bc", [("hll", 1e-3, (0, 0, 0, 0)), ("hllc", 1e-3, (0, 0, 0, 0)),
+                                              ("exact", 1e-3, (0, 0, 0, 0)), ("force", 1e-3, (0, 0, 0, 0)),
+                                              ("hllc", 0.0, (0, 0, 0, 0)), ("hllc", 1e-3, (1, 0, 1, 1)),
+                                              ("exact", 0.0, (1, 1, 0, 1))])
+def test_adjoint_matches_forward_mode(E, harness, tmp_path, solver, smooth, bc):
+    """48x40 grid, 30 CFL steps, checkpoints every 7 (partial last segment):
+    GPU FP64 adjoint = forward-mode derivative to 1e-8 relative."""
+    cfg = geometry(48, 40)
+    rho, p = blast_fields(cfg, smooth)
+    U0 = grid_of(cfg, rho, p)
+    dts = cfl_dts(E, cfg, U0, solver, 30)
+    mask = ring(cfg)
+    dirs = directions(cfg, 4)
+    with E.Solver(cfg, "fp64", solver, bc=bc) as s:
+        s.upload(U0)
+        s.adjoint_forward(dts, 7)
+        g = s.adjoint_backward(dJ_dU(s.download(), mask))
+    ad = adjoint_dirs(g, dirs)
+    fm, cpu_ad = forward_mode(harness, tmp_path, cfg, SOLVER_ID[solver], dts, rho, p, mask,
+                              [d.reshape(-1) for d in dirs], bc)
+    np.testing.assert_allclose(cpu_ad, fm, rtol=1e-12)
+    np.testing.assert_allclose(ad, fm, rtol=1e-8)
+
+
 @pytest.mark.parametrize("solver", ("hll", "hllc", "exact", "force"))
 def test_adjoint_fd_small(E, solver):
-    """48x40 grid, 30 steps, checkpoints every 7 (a partial last segment)."""
-    errs, _ = fd_check(E, geometry(48, 40), solver, 30, 7, 4)
-    assert max(errs) <= 1e-6, errs
-
-
-def test_adjoint_fd_reflective(E):
-    errs, _ = fd_check(E, geometry(40, 36), "hllc", 24, 5, 4, bc=(1, 0, 1, 1))
-    assert max(errs) <= 1e-6, errs
+    """Central differences on the 48x40 case: agreement to the kink-limited
+    level, and the error shrinks as eps does."""
+    cfg = geometry(48, 40)
+    e6, _ = fd_check(E, cfg, solver, 30, 7, 4, eps=1e-6, smooth=2e-2)
+    e7, _ = fd_check(E, cfg, solver, 30, 7, 4, eps=1e-7, smooth=2e-2)
+    print(solver, "fd rel err eps=1e-6", ["%.1e" % e for e in e6], "eps=1e-7", ["%.1e" % e for e in e7])
+    assert np.median(e6) <= 1e-3
+    assert np.median(e7) <= np.median(e6)
 
 
 def test_adjoint_backward_repeatable(E):
@@ -172,24 +249,25 @@ def test_adjoint_forward_matches_step_n(E):
 
 def test_adjoint_config_512(E):
     """The adjoint benchmark geometry: 512^2, HLLC + minmod, 400 frozen-dt
-    steps, checkpoints every 32; FP64 adjoint within 1e-6 of central FD
-    (eps 1e-6, FP64 forward) along 16 seeded Gaussian directions; the FP32
-    adjoint of the FP32 forward against the FP64 adjoint."""
+    steps, checkpoints every 32, 16 seeded Gaussian directions, central
+    differences with eps = 1e-6 of the FP64 forward; the FP32 adjoint of the
+    FP32 forward against the FP64 adjoint."""
     cfg = geometry(512)
-    errs, g64 = fd_check(E, cfg, "hllc", 400, 32, 16)
-    print("fd rel errors", ["%.2e" % e for e in errs])
-    assert max(errs) <= 1e-6, errs
-    rho, p = blast_fields(cfg)
+    errs, g64 = fd_check(E, cfg, "hllc", 400, 32, 16, smooth=2e-2)
+    print("fd rel errors", ["%.2e" % e for e in errs], "median %.2e" % np.median(errs))
+    assert np.median(errs) <= 1e-3
+    rho, p = blast_fields(cfg, 2e-2)
     U0 = grid_of(cfg, rho, p)
     dts = cfl_dts(E, cfg, U0, "hllc", 400)
     with E.Solver(cfg, "fp32", "hllc") as s:
         s.upload(U0)
         s.adjoint_forward(dts, 32)
         g32 = s.adjoint_backward(dJ_dU(s.download(), ring(cfg)))
+        ms = s.adjoint_timing()
     a = np.concatenate([g64[..., 0].ravel(), g64[..., 3].ravel()])
     b = np.concatenate([g32[..., 0].ravel(), g32[..., 3].ravel()])
     rel = np.linalg.norm(a - b) / np.linalg.norm(a)
-    print("fp32 vs fp64 adjoint relative L2", rel)
+    print("fp32 vs fp64 adjoint relative L2 %.3e; fp32 forward %.2f ms, backward %.2f ms" % (rel, ms[0], ms[1]))
     assert rel <= 5e-2
 
 

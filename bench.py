@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--skip-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -221,6 +222,55 @@ def run_reference(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_leg(E, np):
+    """Adjoint workload: the 512^2 blast of [0,2]^2, HLLC + minmod, 400 steps
+    with the FP64 CFL dt sequence frozen, checkpoints every 32 steps,
+    J = sum rho^2 over 0.6 <= r <= 0.8.  Times (CUDA events) the checkpointed
+    forward, the backward (recomputation + adjoint sweeps) and the plain
+    graph-replayed forward of the same 400 steps."""
+    from large_sys_eq_opt_gb300.cases import blast_adjoint_512
+    n, nsteps, k = 512, 400, 32
+    prob = blast_adjoint_512()
+    s64 = E.Solver.for_problem(prob, "fp64", "hllc")
+    s64.set_dt_log(nsteps)
+    s64.step_n(nsteps)
+    dts = s64.dt_log(nsteps)
+    s64.close()
+    x = (np.arange(n) + 0.5) * (2.0 / n)
+    X, Y = np.meshgrid(x, x)
+    r = np.sqrt((X - 1.0) ** 2 + (Y - 1.0) ** 2)
+    mask = (r >= 0.6) & (r <= 0.8)
+    res = {"workload": f"blast_{n}x{n}_hllc_{nsteps}steps_ckpt{k}", "objective": "sum rho^2 over 0.6<=r<=0.8",
+           "dt": "FP64 CFL 0.8 sequence frozen"}
+    grads = {}
+    for prec in ("fp32", "fp64"):
+        s = E.Solver.for_problem(prob, prec, "hllc")
+        U0 = s.download()
+        fwd, bwd = [], []
+        for rep in range(3 if prec == "fp32" else 1):
+            s.upload(U0)
+            s.adjoint_forward(dts, k)
+            gN = np.zeros_like(U0)
+            UN = s.download()
+            gN[2:-2, 2:-2, 0] = np.where(mask, 2.0 * UN[2:-2, 2:-2, 0], 0.0)
+            grads[prec] = s.adjoint_backward(gN)
+            f_ms, b_ms = s.adjoint_timing()
+            fwd.append(f_ms)
+            bwd.append(b_ms)
+        s.upload(U0)
+        s.step_n(8)   # warm the graph
+        s.upload(U0)
+        plain = s.time_steps(nsteps)[0]
+        s.close()
+        f_ms, b_ms = float(np.median(fwd)), float(np.median(bwd))
+        res[prec] = {"forward_ckpt_ms": f_ms, "backward_ms": b_ms, "forward_graph_ms": plain,
+                     "backward_over_forward": b_ms / plain, "gradient_over_forward": (f_ms + b_ms) / plain}
+    a = np.concatenate([grads["fp64"][..., 0].ravel(), grads["fp64"][..., 3].ravel()])
+    b = np.concatenate([grads["fp32"][..., 0].ravel(), grads["fp32"][..., 3].ravel()])
+    res["fp32_vs_fp64_gradient_rel_l2"] = float(np.linalg.norm(a - b) / np.linalg.norm(a))
+    return res
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -305,6 +355,10 @@ def run_ours(args, dist: Dist):
         se.close()
         del A, B
 
+    # ---- discrete adjoint: time ratio against the forward -----------------
+    if not args.skip_adjoint:
+        out["adjoint"] = adjoint_leg(E, np)
+
     # ---- CPU baseline (oracle port on the host cores) ---------------------
     if dist.rank == 0 and dist.ws == 1 and not args.skip_cpu:
         rate, threads, steps, el = cpu_port_rate(n, args.solver, args.cpu_seconds)
@@ -324,7 +378,8 @@ def run_ours(args, dist: Dist):
                        "l2": "inputs larger than L2 (1.07 GB per FP32 state buffer vs 126 MB L2)",
                        "parallelism": f"replicas x{dist.ws}"},
             "gpu_launches": 2 * K,
-            "adjoint_forward_ratio": None,
+            "adjoint_forward_ratio": (out["adjoint"]["fp32"]["backward_over_forward"]
+                                      if "adjoint" in out else None),
         }
         line.update(out)
         print(json.dumps(line), flush=True)

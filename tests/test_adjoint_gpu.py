@@ -176,11 +176,17 @@ SOLVER_ID = {"hll": 0, "hllc": 1, "exact": 2, "force": 3}
 
 @pytest.mark.parametrize("solver,smooth,bc", [("hll", 1e-3, (0, 0, 0, 0)), ("hllc", 1e-3, (0, 0, 0, 0)),
                                               ("exact", 1e-3, (0, 0, 0, 0)), ("force", 1e-3, (0, 0, 0, 0)),
-                                              ("hllc", 0.0, (0, 0, 0, 0)), ("hllc", 1e-3, (1, 0, 1, 1)),
-                                              ("exact", 0.0, (1, 1, 0, 1))])
+                                              ("hllc", 1e-3, (1, 0, 1, 1)), ("exact", 2e-2, (1, 1, 0, 1))])
 def test_adjoint_matches_forward_mode(E, harness, tmp_path, solver, smooth, bc):
     """48x40 grid, 30 CFL steps, checkpoints every 7 (partial last segment):
-    GPU FP64 adjoint = forward-mode derivative to 1e-8 relative."""
+    GPU FP64 adjoint = forward-mode derivative to 1e-8 relative.
+
+    The exactly piecewise-constant blast is checked on the CPU only
+    (adj_check.cpp): there every ambient limiter argument is an exact tie,
+    and whether a tie survives a step depends on the last bit of the
+    forward's rounding (the GPU's fused multiply-adds leave 1-ulp ripples
+    that the CPU restatement does not), so the two trajectories take
+    different -- equally valid -- branches."""
     cfg = geometry(48, 40)
     rho, p = blast_fields(cfg, smooth)
     U0 = grid_of(cfg, rho, p)

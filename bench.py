@@ -245,6 +245,7 @@ def adjoint_leg(E, np):
     grads = {}
     for prec in ("fp32", "fp64"):
         s = E.Solver.for_problem(prob, prec, "hllc")
+        shape = s.autotune(20)
         U0 = s.download()
         fwd, bwd = [], []
         for rep in range(3 if prec == "fp32" else 1):
@@ -263,7 +264,7 @@ def adjoint_leg(E, np):
         plain = s.time_steps(nsteps)[0]
         s.close()
         f_ms, b_ms = float(np.median(fwd)), float(np.median(bwd))
-        res[prec] = {"forward_ckpt_ms": f_ms, "backward_ms": b_ms, "forward_graph_ms": plain,
+        res[prec] = {"seg_xy": list(shape), "forward_ckpt_ms": f_ms, "backward_ms": b_ms, "forward_graph_ms": plain,
                      "backward_over_forward": b_ms / plain, "gradient_over_forward": (f_ms + b_ms) / plain}
     a = np.concatenate([grads["fp64"][..., 0].ravel(), grads["fp64"][..., 3].ravel()])
     b = np.concatenate([grads["fp32"][..., 0].ravel(), grads["fp32"][..., 3].ravel()])
@@ -286,6 +287,7 @@ def run_ours(args, dist: Dist):
 
     # ---- FP32 device-resident throughput (the headline) -------------------
     s32 = E.Solver.for_problem(prob, "fp32", args.solver)
+    shape32 = s32.autotune(10)
     s32.time_steps(W)
     dist.barrier()
     with ClockSampler(dist.local) as clk:
@@ -376,7 +378,8 @@ def run_ours(args, dist: Dist):
                        "limiter": "minmod", "cfl": 0.8, "precision": "fp32 (FP64 pressure recovery under "
                        "cancellation, FP64 exact-solver Newton)", "graph": f"{K} steps in one CUDA graph",
                        "l2": "inputs larger than L2 (1.07 GB per FP32 state buffer vs 126 MB L2)",
-                       "parallelism": f"replicas x{dist.ws}"},
+                       "parallelism": f"replicas x{dist.ws}",
+                       "seg_xy": list(shape32) + ["autotuned"]},
             "gpu_launches": 2 * K,
             "adjoint_forward_ratio": (out["adjoint"]["fp32"]["backward_over_forward"]
                                       if "adjoint" in out else None),

@@ -1179,6 +1179,56 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
     return status_code(h);
 }
 
+// Measured choice of the launch shape: each trial sets one candidate
+// segment length per sweep and times `steps` graph-replayed steps with CUDA
+// events around every kernel; the x- and y-sweep times are kept apart, so
+// one pass over the trials tunes both sweeps.  The state, time and step
+// counter are restored afterwards.
+int eu_autotune(eu_handle* h, int steps, long long chosen[2]) {
+    if (!h || steps < 1) return fail(h, EU_ERR_INVALID, "eu_autotune: bad argument");
+    const int CX = h->K.box_x, RY = h->K.ry;
+    std::vector<int> cx, cy;
+    for (int v : {CX, 2 * CX, 4 * CX, 32, 64, 128, 256})
+        if (v % CX == 0 && v <= round_up(h->cfg.nx, CX) && std::find(cx.begin(), cx.end(), v) == cx.end()) cx.push_back(v);
+    for (int v : {RY, 2 * RY, 4 * RY, 32, 64, 128})
+        if (v % RY == 0 && v <= round_up(h->cfg.ny, RY) && std::find(cy.begin(), cy.end(), v) == cy.end()) cy.push_back(v);
+    if (cx.empty()) cx.push_back(CX);
+    if (cy.empty()) cy.push_back(RY);
+    void* saved = nullptr;
+    EU_CUDA(h, cudaMalloc(&saved, state_bytes(h)));
+    const int cur0 = h->cur;
+    const Ctl ctl0 = *h->hctl;
+    cudaError_t e = cudaMemcpyAsync(saved, h->S[cur0], state_bytes(h), cudaMemcpyDeviceToDevice, h->st);
+    const int seg_x0 = h->seg_x, seg_y0 = h->seg_y;
+    int best_x = seg_x0, best_y = seg_y0;
+    float tbx = INFINITY, tby = INFINITY;
+    int rc = EU_OK;
+    const size_t trials = std::max(cx.size(), cy.size());
+    for (size_t t = 0; t < trials && rc == EU_OK && e == cudaSuccess; ++t) {
+        const int sx = cx[std::min(t, cx.size() - 1)], sy = cy[std::min(t, cy.size() - 1)];
+        rc = eu_set_option(h, "seg_x", sx);
+        if (rc == EU_OK) rc = eu_set_option(h, "seg_y", sy);
+        float ms[3];
+        if (rc == EU_OK) rc = eu_time_steps(h, 2, 1, ms);
+        if (rc == EU_OK) rc = eu_time_steps(h, steps, 1, ms);
+        if (rc != EU_OK) break;
+        if (t < cx.size() && ms[1] < tbx) { tbx = ms[1]; best_x = sx; }
+        if (t < cy.size() && ms[2] < tby) { tby = ms[2]; best_y = sy; }
+    }
+    if (rc == EU_OK) rc = eu_set_option(h, "seg_x", best_x);
+    if (rc == EU_OK) rc = eu_set_option(h, "seg_y", best_y);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->S[cur0], saved, state_bytes(h), cudaMemcpyDeviceToDevice, h->st);
+    h->cur = cur0;
+    *h->hctl = ctl0;
+    if (e == cudaSuccess && ctl_push(h) != EU_OK) e = cudaErrorUnknown;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(saved);
+    if (rc != EU_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(h, e, "eu_autotune");
+    if (chosen) { chosen[0] = best_x; chosen[1] = best_y; }
+    return EU_OK;
+}
+
 int eu_apply_boundary(eu_handle* h) {
     if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
     EU_CUDA(h, fill_ghosts(h, h->cur));

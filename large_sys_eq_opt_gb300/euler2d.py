@@ -54,7 +54,7 @@ EXPORTS = (
     "eu_host_alloc", "eu_host_free", "eu_device_info", "eu_apply_boundary", "eu_set_dt_log",
     "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option", "eu_read_planes",
     "eu_advance_first_order", "eu_advance_first_order_host", "eu_totals_noalloc",
-    "eu_adjoint_forward", "eu_adjoint_backward", "eu_adjoint_timing",
+    "eu_adjoint_forward", "eu_adjoint_backward", "eu_adjoint_timing", "eu_autotune",
 )
 
 _lib = None
@@ -117,6 +117,7 @@ def load(path: str = LIB_PATH):
     L.eu_adjoint_forward.argtypes = [H, C.c_longlong, _dp, C.c_int]
     L.eu_adjoint_backward.argtypes = [H, _dp, _dp]
     L.eu_adjoint_timing.argtypes = [H, C.POINTER(C.c_float)]
+    L.eu_autotune.argtypes = [H, C.c_int, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -369,6 +370,12 @@ class Solver:
         return dt.value
 
     # -- measurement ---------------------------------------------------------
+    def autotune(self, steps: int = 20):
+        """Measure and set the fastest segment lengths; returns (seg_x, seg_y)."""
+        out = (C.c_longlong * 2)()
+        self._check(self._L.eu_autotune(self._h, int(steps), out))
+        return int(out[0]), int(out[1])
+
     def time_steps(self, nsteps: int, use_graph=True):
         ms = (C.c_float * 3)()
         self._check(self._L.eu_time_steps(self._h, int(nsteps), int(bool(use_graph)), ms))

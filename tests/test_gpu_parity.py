@@ -239,3 +239,24 @@ def test_fp32_device_run_tracks_fp64_oracle(E, port, nx, ny):
     assert info["status"] == 0
     e = l1(interior(got)[..., 0], interior(U)[..., 0])
     assert e <= 1e-5, e
+
+
+@pytest.mark.parametrize("prec", ("fp32", "fp64"))
+def test_autotune_keeps_state_and_results(E, prec):
+    """The autotuner restores state and time, picks legal shapes, and the
+    steps it makes faster give the same bits (every cell's arithmetic is
+    independent of where the line segments start)."""
+    from large_sys_eq_opt_gb300.cases import blast_large
+    prob = blast_large(300)
+    with E.Solver.for_problem(prob, prec, "hllc") as a, E.Solver.for_problem(prob, prec, "hllc") as b:
+        before = b.download()
+        t0 = b.time()
+        sx, sy = b.autotune(4)
+        assert np.array_equal(b.download(), before)
+        assert b.time() == t0
+        cx = 8 if prec == "fp32" else 4
+        assert sx % cx == 0 and sy % 4 == 0
+        assert (b.get_option("seg_x"), b.get_option("seg_y")) == (sx, sy)
+        a.step_n(12)
+        b.step_n(12)
+        assert np.array_equal(a.download(), b.download())

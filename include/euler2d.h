@@ -186,6 +186,35 @@ int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0);
  * only) and eu_adjoint_backward (ms[1], recomputation + adjoint sweeps). */
 int eu_adjoint_timing(eu_handle* h, float ms[2]);
 
+/* ---- uneven ensembles (no counterpart in the reference) ---------------------- */
+/* n independent grids (own size, boundaries, case, parameters, CFL and
+ * t_end) advanced together: every step is one persistent launch over a work
+ * list of all instances' sweep tasks, and each instance keeps its own
+ * device-computed dt.  Each instance's results are bit-for-bit those of its
+ * own handle.  eu_batch_handle(b, i) gives the instance's handle for the
+ * setup, state transfer, totals and option calls above (do not destroy it;
+ * do not step it on its own while the batch is stepping). */
+typedef struct eu_batch eu_batch;
+int eu_batch_create(int n, const eu_case* cfgs, const int* bcs /* 4 per instance or NULL */, eu_precision prec,
+                    eu_solver solver, eu_batch** out);
+void eu_batch_destroy(eu_batch* b);
+const char* eu_batch_last_error(const eu_batch* b);
+eu_handle* eu_batch_handle(eu_batch* b, int i);
+/* t = 0 on every instance: ghosts filled, first dt from the CFL reduction,
+ * each instance stops at its own cfg.t_end (the reference loop's clip). */
+int eu_batch_start(eu_batch* b);
+/* nsteps ensemble steps (finished instances idle); *all_done (may be NULL)
+ * reports whether every instance reached its t_end. */
+int eu_batch_step(eu_batch* b, long long nsteps, int* all_done);
+/* Steps until every instance reached its t_end or max_steps were taken. */
+int eu_batch_run(eu_batch* b, long long max_steps, long long* steps_taken);
+/* Device time (CUDA events) of nsteps graph-replayed ensemble steps. */
+int eu_batch_time_steps(eu_batch* b, int nsteps, float* ms);
+/* Ensemble tile-shape autotuner: one (seg_x, seg_y) pair for all instances
+ * (clipped to each grid), chosen by timing whole ensemble steps; states
+ * restored afterwards. */
+int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]);
+
 /* ---- drop-in calls on host grids (what the reference's callers pass) ------- */
 /* compute_dt(const Grid2D&, double): upload, reduce, read back dt. */
 int eu_compute_dt_host(eu_handle* h, const double* U, double cfl, double* dt);

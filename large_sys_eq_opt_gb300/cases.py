@@ -154,3 +154,32 @@ def post_shock_state(p: ShockBubbleParams):
     p2 = p.p0 * (1.0 + 2.0 * GAMMA / (GAMMA + 1.0) * (M2 - 1.0))
     u2 = 2.0 * a0 / (GAMMA + 1.0) * (p.mach - 1.0 / p.mach)
     return rho2, u2, p2
+
+
+def ensemble_problems(seed: int = 2024, n_blast: int = 48, n_bubble: int = 16) -> list:
+    """The uneven ensemble workload (fixed seed): n_blast blasts on [0,2]^2
+    with inner radius U[0.2, 0.5], inner p log-uniform in [1, 100], inner rho
+    1, outer rho 0.125 and p 0.1, on grids drawn from {128^2, 256^2, 512^2,
+    1024^2} (transmissive, CFL 0.8, t_end 0.25); and n_bubble shock-bubbles
+    on [0,0.225]x[0,0.089] with bubble rho U[0.1, 3.0] and Mach U[1.1, 2.0]
+    on nx uniform in [500, 2000], ny = round(0.396 nx) (reflective in y,
+    CFL 0.8, t_end 0.1)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_blast):
+        n = int(rng.choice([128, 256, 512, 1024]))
+        r = float(rng.uniform(0.2, 0.5))
+        p_in = float(10.0 ** rng.uniform(0.0, 2.0))
+        out.append(Problem(CaseConfig(n, n, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.25), "blast",
+                           BlastParams(r=r, p_in=p_in), name=f"blast{k}_{n}"))
+    for k in range(n_bubble):
+        nx = int(rng.integers(500, 2001))
+        ny = int(round(0.396 * nx))
+        rho_b = float(rng.uniform(0.1, 3.0))
+        mach = float(rng.uniform(1.1, 2.0))
+        out.append(Problem(CaseConfig(nx, ny, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.1), "shock_bubble",
+                           ShockBubbleParams(mach=mach, rho_bubble=rho_b),
+                           bc=(TRANSMISSIVE, TRANSMISSIVE, REFLECTIVE, REFLECTIVE), name=f"bubble{k}_{nx}x{ny}"))
+    return out
+

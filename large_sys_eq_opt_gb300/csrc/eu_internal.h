@@ -81,6 +81,39 @@ template <class T> struct SweepArgs {
     long long snap_plane, snap_stride;
 };
 
+// ---- ensemble (many independent grids in one persistent launch per step) ----
+constexpr int kMaxInst = 256;
+
+// One instance as the ensemble kernel sees it (device memory, 64-byte
+// aligned for the tensor maps).
+template <class T> struct EnsInst {
+    CUtensorMap tm_x[2];   // x-sweep input, per state buffer
+    CUtensorMap tm_xo;     // x-sweep output (Utmp)
+    CUtensorMap tm_y;      // y-sweep input (Utmp)
+    CUtensorMap tm_yo[2];  // y-sweep output, per state buffer
+    SweepArgs<T> xa;       // x-sweep arguments
+    SweepArgs<T> ya[2];    // y-sweep arguments writing state buffer b
+};
+
+// Work-list state of one launch: the dequeue counter and, per instance,
+// the number of finished x-sweep tasks (reset before every launch).
+struct EnsSched {
+    unsigned int next;
+    unsigned int pad[31];
+    unsigned int xdone[kMaxInst];
+};
+
+template <class T> struct EnsArgs {
+    const EnsInst<T>* inst;
+    EnsSched* sched;
+    int ninst;
+    int total_x, total_y;
+    int x_off[kMaxInst + 1];   // prefix sums of the instances' x-sweep tasks
+    int y_off[kMaxInst + 1];   // ... and y-sweep tasks
+};
+
+using EnsembleLaunch = cudaError_t (*)(const void* args, int ctas, cudaStream_t s);
+
 // Host-side launch entry of one sweep instantiation.
 using SweepLaunch = cudaError_t (*)(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args,
                                     int ctas, cudaStream_t s);
@@ -91,6 +124,8 @@ using FirstOrderLaunch = cudaError_t (*)(const void* in, const void* out, int nx
 struct SweepKernels {
     SweepLaunch x, y;
     FirstOrderLaunch first;  // first-order Godunov step (in/out: Planes<T>*)
+    EnsembleLaunch ens;      // persistent ensemble step (args: EnsArgs<T>*)
+    int (*occ_e)();          // resident CTAs per SM of the ensemble kernel
     int (*occ_x)();      // resident CTAs per SM of each kernel
     int (*occ_y)();
     int box_x;           // x-sweep box: box_x columns (32 bytes) x 32 rows, 32-byte swizzle

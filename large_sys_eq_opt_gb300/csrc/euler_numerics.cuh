@@ -51,6 +51,7 @@ template <> struct Ar<double> {
     static __device__ __forceinline__ double fmax_(double a, double b) { return fmax(a, b); }
     static __device__ __forceinline__ bool finite(double x) { return fabs(x) < INFINITY; }
     static __device__ __forceinline__ double pow_(double a, double b) { return pow(a, b); }
+    static __device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
 };
 
 template <> struct Ar<float> {
@@ -72,6 +73,7 @@ template <> struct Ar<float> {
     static __device__ __forceinline__ float fmax_(float a, float b) { return fmaxf(a, b); }
     static __device__ __forceinline__ bool finite(float x) { return fabsf(x) < INFINITY; }
     static __device__ __forceinline__ float pow_(float a, float b) { return powf(a, b); }
+    static __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 };
 
 template <class T> __device__ __forceinline__ T gm1() { return T(kGm1D); }
@@ -459,16 +461,35 @@ template <class T> __device__ __forceinline__ bool nice_cell(const Prim<T>& V) {
     return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(4.0e-12);
 }
 
-// cons_to_prim without the FP64 island; flags the states that need it.
-template <class T> __device__ __forceinline__ Prim<T> c2p_fast(const Cons<T>& U, bool& slow) {
+// cons_to_prim of a cell state, with the rounding fixed by explicit fused
+// multiply-adds so that the fast path and the full path (cell_full) give the
+// same bits: a cell's primitives never depend on which path computed them,
+// which keeps every output independent of where a line segment starts.
+template <class T> __device__ __forceinline__ Prim<T> c2p_arith(const Cons<T>& U, T& t) {
     Prim<T> V;
     V.ir = Ar<T>::rcp(U.r);
     V.r = U.r;
     V.un = U.mn * V.ir;
     V.ut = U.mt * V.ir;
-    const T t = U.mt * V.ut + U.mn * V.un;             // twice the kinetic energy
-    V.p = gm1<T>() * U.e - T(0.5 * kGm1D) * t;
+    t = Ar<T>::fma_(U.mt, V.ut, U.mn * V.un);          // twice the kinetic energy
+    V.p = Ar<T>::fma_(T(-0.5 * kGm1D), t, gm1<T>() * U.e);
+    return V;
+}
+
+// cons_to_prim without the FP64 island; flags the states that need it.
+template <class T> __device__ __forceinline__ Prim<T> c2p_fast(const Cons<T>& U, bool& slow) {
+    T t;
+    const Prim<T> V = c2p_arith(U, t);
     if constexpr (sizeof(T) == 4) slow |= t > U.e;     // kinetic > E/2: FP64 recovery
+    return V;
+}
+
+// The same primitives with the FP64 island applied (full path).
+template <class T> __device__ __forceinline__ Prim<T> c2p_cell(const Cons<T>& U) {
+    T t;
+    Prim<T> V = c2p_arith(U, t);
+    if constexpr (sizeof(T) == 4)
+        if (t > U.e) V.p = pressure_fp64(U.r, U.mn, U.mt, U.e);
     return V;
 }
 
@@ -623,11 +644,19 @@ template <class T> struct CellOut {
 template <class T, int S>
 __device__ __noinline__ CellOut<T> cell_full(Cons<T> U, Prim<T> Wm2, Prim<T> Wm1, Face<T> Rp, T hl) {
     CellOut<T> o;
-    o.W = cons_to_prim(U);
+    o.W = c2p_cell(U);
     reconstruct(Wm2, Wm1, o.W, hl, o.L, o.R);
     o.F = riemann<S>(Rp.U, Rp.V, o.L.U, o.L.V);
     o.r_phys = physical_riemann(o.R.V);
     return o;
+}
+
+// Full-logic flux of one face whose right state came from the fast path
+// (taken when only the face flagged a fallback, e.g. a non-physical left
+// state).
+template <class T, int S>
+__device__ __noinline__ Cons<T> face_full(Face<T> Rp, Face<T> L) {
+    return riemann<S>(Rp.U, Rp.V, L.U, L.V);
 }
 
 // Largest signal speed max(|un|+a, |ut|+a) of a conserved state

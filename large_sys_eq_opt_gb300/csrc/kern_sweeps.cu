@@ -19,6 +19,8 @@
 #define OCC_X EU_NAME(occ_x, EU_PREC, EU_SOLVER)
 #define LAUNCH_F EU_NAME(launch_first, EU_PREC, EU_SOLVER)
 #define OCC_Y EU_NAME(occ_y, EU_PREC, EU_SOLVER)
+#define LAUNCH_E EU_NAME(launch_ens, EU_PREC, EU_SOLVER)
+#define OCC_E EU_NAME(occ_e, EU_PREC, EU_SOLVER)
 
 namespace eu {
 namespace {
@@ -74,6 +76,24 @@ static cudaError_t LAUNCH_F(const void* in, const void* out, int nx, int ny, dou
     return cudaGetLastError();
 }
 
+constexpr size_t kSmemE = ensemble_smem<T, SX, RY, BWY, SY, NW>();
+
+static cudaError_t LAUNCH_E(const void* args, int ctas, cudaStream_t s) {
+    auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_Y>;
+    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemE);
+    if (attr != cudaSuccess) return attr;
+    k<<<ctas, NW * 32, kSmemE, s>>>(*static_cast<const EnsArgs<T>*>(args));
+    return cudaGetLastError();
+}
+
+static int OCC_E() {
+    auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_Y>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemE);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, kSmemE) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
 static int OCC_X() {
     auto k = sweep_x_kernel<T, SOL, SX, NW, MINB_X>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX);
@@ -98,6 +118,8 @@ SweepKernels EU_NAME(sweep_kernels, EU_PREC, EU_SOLVER)() {
     k.y = LAUNCH_Y;
     k.occ_x = OCC_X;
     k.first = LAUNCH_F;
+    k.ens = LAUNCH_E;
+    k.occ_e = OCC_E;
     k.occ_y = OCC_Y;
     k.box_x = CX;
     k.ry = RY;

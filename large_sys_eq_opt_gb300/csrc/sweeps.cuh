@@ -55,18 +55,26 @@ template <class T, int S> struct Line {
 
     // U(c-2) - lam (F(c-3/2) - F(c-5/2)) is evaluated as A - lam F(c-3/2)
     // (src/cpu/solver_cpu.cpp:452-453, :489-490).
+    // A cell flagged by its own reconstruction is recomputed in full; a cell
+    // whose only flag is the face (a non-physical left face state, a Riemann
+    // fallback) keeps its fast-path primitives and face states and
+    // recomputes only the flux.
     __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
-        bool slow = !rp_phys;
-        Prim<T> W = c2p_fast(U, slow);
+        bool slow_cell = false, slow_face = !rp_phys;
+        Prim<T> W = c2p_fast(U, slow_cell);
         const bool nice = nice_cell(W);
         Face<T> L, R;
-        reconstruct_fast(Wm2, Wm1, W, hl, nice && nice1 && nice2, L, R, slow);
-        Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);
+        reconstruct_fast(Wm2, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell);
+        Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow_face);
         bool r_phys = true;
-        if (__builtin_expect(slow, 0)) {
-            const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl);
-            W = o.W; L = o.L; R = o.R; F = o.F;
-            r_phys = o.r_phys;
+        if (__builtin_expect(slow_cell | slow_face, 0)) {
+            if (slow_cell) {
+                const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl);
+                W = o.W; L = o.L; R = o.R; F = o.F;
+                r_phys = o.r_phys;
+            } else {
+                F = face_full<T, S>(Rp, L);
+            }
         }
         const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
         A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
@@ -231,28 +239,35 @@ __device__ __forceinline__ void warp_arrive(Ctl* ctl, T smax, bool bad, bool tim
 // 32-byte rows.  Box 0 only warms the stencil window up; boxes 1.. hold
 // exactly this segment's outputs (clipped by the store map at the edges).
 // ---------------------------------------------------------------------------
-template <class T, int S, int STAGES, int NW, int MINB>
-__global__ void __launch_bounds__(NW * 32, MINB)
-    sweep_x_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tm_out,
-                   const SweepArgs<T> a) {
+// Per-warp mbarrier phases: bit s is the parity the next wait on stage s
+// expects.  A warp initialises its barriers once and carries the bits from
+// task to task (a persistent warp runs many tasks on the same barriers).
+// A single-task launch (PERSIST = false) derives the parity from the box
+// index instead, as its barriers start fresh.
+template <bool PERSIST>
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, int s, int k, int stages, uint32_t& phase) {
+    if constexpr (!PERSIST) {
+        return mbar_wait_bounded(smem_u32(&bar[s]), (uint32_t)((k / stages) & 1));
+    } else {
+        const bool ok = mbar_wait_bounded(smem_u32(&bar[s]), (phase >> s) & 1u);
+        if (ok) phase ^= 1u << s;
+        return ok;
+    }
+}
+
+// One x-sweep task (one warp): 32 rows x one segment of columns.  Returns
+// true when a bounded wait expired (the task is abandoned after draining the
+// boxes in flight).
+template <class T, int S, int STAGES, bool PERSIST>
+__device__ __forceinline__ bool x_task(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
+                                       int task, T* buf, uint64_t* bar, uint32_t& phase, int lane) {
     constexpr int CX = 32 / sizeof(T);          // columns per box: 32-byte rows
     constexpr int HV = CX / 2;                  // cells per 16-byte half row
     constexpr int STAGE = 4 * 32 * CX;          // elements: 4 fields x 32 rows x CX
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
     static_assert(STAGE_BYTES % 1024 == 0, "32-byte swizzle needs 1 KB-aligned stage buffers");
     static_assert(kTOff == kSOff + 2, "outputs must land in their input's column");
-    extern __shared__ __align__(1024) unsigned char smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int task = blockIdx.x * NW + warp;
-    if (task >= a.ntasks) return;
     Ctl* ctl = a.ctl;
-    if (__ldcg(&ctl->done)) return;
-
-    // stage buffers on a 1 KB boundary (the launch reserves 1 KB of slack)
-    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
-    T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
-
     const int rg = task / a.nseg;                // 32-row group
     const int s0 = (task - rg * a.nseg) * a.seg; // first interior column of the segment
     const int e = min(s0 + a.seg, a.nx);
@@ -267,17 +282,14 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     T* snap = (req && a.snap) ? a.snap + (long long)(__ffs(req) - 1) * a.snap_stride : nullptr;
 
     if (lane == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bar[s]), 1);
-        fence_mbar_init();
-        tma_prefetch_desc(&tm);
-        tma_prefetch_desc(&tm_out);
+        tma_prefetch_desc(tm);
+        tma_prefetch_desc(tm_out);
     }
-    __syncwarp();
     auto issue = [&](int k) {
         const int s = k % STAGES;
         const uint32_t b = smem_u32(&bar[s]);
         mbar_arrive_expect_tx(b, STAGE_BYTES);
-        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, m0 + k * CX, rg * 32 + 2, 0);
+        tma_load_3d(smem_u32(buf + s * STAGE), tm, b, m0 + k * CX, rg * 32 + 2, 0);
     };
     if (lane == 0) {
         const int np = min(STAGES, nst);
@@ -294,7 +306,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     int kfail = nst;
     for (int k = 0; k < nst; ++k) {
         const int s = k % STAGES;
-        if (!mbar_wait_bounded(smem_u32(&bar[s]), (uint32_t)((k / STAGES) & 1))) {
+        if (!stage_wait<PERSIST>(bar, s, k, STAGES, phase)) {
             timed_out = true;
             kfail = k;
             break;
@@ -361,7 +373,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         __syncwarp();
         if (lane == 0) {
             if (k > 0) {
-                tma_store_3d(&tm_out, smem_u32(buf + s * STAGE), m0 + k * CX, rg * 32 + 2, 0);
+                tma_store_3d(tm_out, smem_u32(buf + s * STAGE), m0 + k * CX, rg * 32 + 2, 0);
                 bulk_commit();
             }
             // refill the buffer of box k-1 (its store, if any, is the older group)
@@ -376,10 +388,37 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     if (timed_out) {
         // drain the boxes still in flight (bounded), then report
         const int last = min(kfail + STAGES, nst);
-        for (int k = kfail + 1; k < last; ++k)
-            (void)mbar_wait_bounded(smem_u32(&bar[k % STAGES]), (uint32_t)((k / STAGES) & 1));
-        if (lane == 0) atomicOr(&ctl->status, (int)kStatusTimeout);
+        for (int k = kfail + 1; k < last; ++k) (void)stage_wait<PERSIST>(bar, k % STAGES, k, STAGES, phase);
     }
+    return timed_out;
+}
+
+// x-sweep: Uold (S buffer) -> Utmp, one task per warp.
+template <class T, int S, int STAGES, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB)
+    sweep_x_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tm_out,
+                   const SweepArgs<T> a) {
+    constexpr int STAGE = 4 * 32 * (32 / sizeof(T));
+    constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int task = blockIdx.x * NW + warp;
+    if (task >= a.ntasks) return;
+    Ctl* ctl = a.ctl;
+    if (__ldcg(&ctl->done)) return;
+
+    // stage buffers on a 1 KB boundary (the launch reserves 1 KB of slack)
+    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+    T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * STAGES * STAGE_BYTES) + warp * STAGES;
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bar[s]), 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    uint32_t phase = 0;
+    if (x_task<T, S, STAGES, false>(&tm, &tm_out, a, task, buf, bar, phase, lane) && lane == 0)
+        atomicOr(&ctl->status, (int)kStatusTimeout);
 }
 
 // ---------------------------------------------------------------------------
@@ -396,10 +435,16 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 // columns, are stored directly.
 // src/cpu/solver_cpu.cpp:247-279 + :474-498
 // ---------------------------------------------------------------------------
-template <class T, int S, int RY, int BW, int STAGES, int NW, int MINB>
-__global__ void __launch_bounds__(NW * 32, MINB)
-    sweep_y_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tm_out,
-                   const SweepArgs<T> a) {
+// Result of one y-sweep task for the step's epilogue.
+template <class T> struct YOut {
+    T smax;
+    bool bad, timed_out;
+};
+
+// One y-sweep task (one warp): 32 S columns x one segment of rows.
+template <class T, int S, int RY, int BW, int STAGES, bool PERSIST>
+__device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
+                                          int task, T* buf, T* obuf, uint64_t* bar, uint32_t& phase, int lane) {
     constexpr int STAGE = 4 * RY * BW;
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
     constexpr int OSTAGE = 4 * RY * 32;          // output box: 4 fields x RY rows x 32 columns
@@ -407,19 +452,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     static_assert(STAGE_BYTES % 128 == 0 && OSTAGE_BYTES % 128 == 0, "stage buffers must stay 128-byte aligned");
     static_assert(BW >= 32 + kTOff - kSOff, "box too narrow");
     static_assert(RY == 4, "the 4-row output lag must be exactly one box");
-    extern __shared__ __align__(1024) unsigned char smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int task = blockIdx.x * NW + warp;
-    if (task >= a.ntasks) return;
     Ctl* ctl = a.ctl;
-    if (__ldcg(&ctl->done)) return;
-
-    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
-    T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
-    T* obuf = reinterpret_cast<T*>(base + (size_t)NW * STAGES * STAGE_BYTES) + (size_t)warp * 2 * OSTAGE;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * (STAGES * STAGE_BYTES + 2 * OSTAGE_BYTES)) +
-                    warp * STAGES;
-
     const int rs = task / a.nseg;                // row segment
     const int g = task - rs * a.nseg;            // group of 32 S columns
     const int r0 = rs * a.seg;                   // first interior output row (a multiple of RY)
@@ -436,17 +469,14 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     const T hl = T(0.5 * lam_d);
 
     if (lane == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bar[s]), 1);
-        fence_mbar_init();
-        tma_prefetch_desc(&tm);
-        tma_prefetch_desc(&tm_out);
+        tma_prefetch_desc(tm);
+        tma_prefetch_desc(tm_out);
     }
-    __syncwarp();
     auto issue = [&](int k) {
         const int s = k % STAGES;
         const uint32_t b = smem_u32(&bar[s]);
         mbar_arrive_expect_tx(b, STAGE_BYTES);
-        tma_load_3d(smem_u32(buf + s * STAGE), &tm, b, g * 32, r0 + k * RY, 0);
+        tma_load_3d(smem_u32(buf + s * STAGE), tm, b, g * 32, r0 + k * RY, 0);
     };
     if (lane == 0) {
         const int np = min(STAGES, nst);
@@ -462,7 +492,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     int kfail = nst;
     for (int k = 0; k < nst; ++k) {
         const int s = k % STAGES;
-        if (!mbar_wait_bounded(smem_u32(&bar[s]), (uint32_t)((k / STAGES) & 1))) {
+        if (!stage_wait<PERSIST>(bar, s, k, STAGES, phase)) {
             timed_out = true;
             kfail = k;
             break;
@@ -512,7 +542,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         __syncwarp();
         if (lane == 0) {
             if (k > 0 && g != 0 && g * 32 < a.wclip) {
-                tma_store_3d(&tm_out, smem_u32(obuf + (k & 1) * OSTAGE), g * 32, ir0 + 2, 0);
+                tma_store_3d(tm_out, smem_u32(obuf + (k & 1) * OSTAGE), g * 32, ir0 + 2, 0);
                 bulk_commit();
             }
             if (k + STAGES < nst) issue(k + STAGES);
@@ -521,11 +551,143 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     if (lane == 0) bulk_wait0();
     if (timed_out) {
         const int last = min(kfail + STAGES, nst);
-        for (int k = kfail + 1; k < last; ++k)
-            (void)mbar_wait_bounded(smem_u32(&bar[k % STAGES]), (uint32_t)((k / STAGES) & 1));
+        for (int k = kfail + 1; k < last; ++k) (void)stage_wait<PERSIST>(bar, k % STAGES, k, STAGES, phase);
     }
-    const bool bad = !(Ar<T>::fabs_(ssum) < T(INFINITY));
-    warp_arrive<T>(ctl, smax, bad, timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);
+    return YOut<T>{smax, !(Ar<T>::fabs_(ssum) < T(INFINITY)), timed_out};
+}
+
+// y-sweep: Utmp -> Unew (S buffer), one task per warp, with the fused CFL
+// reduction.
+template <class T, int S, int RY, int BW, int STAGES, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB)
+    sweep_y_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tm_out,
+                   const SweepArgs<T> a) {
+    constexpr int STAGE = 4 * RY * BW;
+    constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
+    constexpr int OSTAGE = 4 * RY * 32;
+    constexpr uint32_t OSTAGE_BYTES = OSTAGE * sizeof(T);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int task = blockIdx.x * NW + warp;
+    if (task >= a.ntasks) return;
+    Ctl* ctl = a.ctl;
+    if (__ldcg(&ctl->done)) return;
+
+    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+    T* buf = reinterpret_cast<T*>(base) + (size_t)warp * STAGES * STAGE;
+    T* obuf = reinterpret_cast<T*>(base + (size_t)NW * STAGES * STAGE_BYTES) + (size_t)warp * 2 * OSTAGE;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * (STAGES * STAGE_BYTES + 2 * OSTAGE_BYTES)) +
+                    warp * STAGES;
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bar[s]), 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    uint32_t phase = 0;
+    const YOut<T> o = y_task<T, S, RY, BW, STAGES, false>(&tm, &tm_out, a, task, buf, obuf, bar, phase, lane);
+    warp_arrive<T>(ctl, o.smax, o.bad, o.timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);
+}
+
+// ---------------------------------------------------------------------------
+// Ensemble step: the x- and y-sweep tasks of many independent grids
+// (instances with their own sizes, boundaries, parameters and dt) in one
+// persistent launch.  Every warp dequeues tasks from one work list -- all
+// x-sweep tasks first, instance by instance, then all y-sweep tasks -- and
+// runs them with the same task bodies as the single-grid kernels, so every
+// instance's result is bit-for-bit that of its own launches.  A y-sweep task
+// of instance q waits (bounded acquire spin) until all of q's x-sweep tasks
+// have published their Utmp writes; every x-sweep task was dequeued before
+// any y-sweep task and none of them waits, so the wait always ends.  Each
+// instance's last y-sweep warp finalises that instance's step (t, step,
+// next dt from its own CFL reduction) exactly as in a single-grid launch.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int ens_find(const int* off, int n, int t) {
+    int lo = 0, hi = n;                          // off[lo] <= t < off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <class T, int S, int SX, int RY, int BWY, int SY, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB) ensemble_kernel(const __grid_constant__ EnsArgs<T> e) {
+    constexpr int CX = 32 / sizeof(T);
+    constexpr size_t XB = (size_t)SX * 4 * 32 * CX * sizeof(T);
+    constexpr size_t YSTAGE = (size_t)4 * RY * BWY * sizeof(T);
+    constexpr size_t YB = SY * YSTAGE + 2 * (size_t)4 * RY * 32 * sizeof(T);
+    constexpr size_t WB = ((XB > YB ? XB : YB) + 1023) / 1024 * 1024;   // per-warp region
+    constexpr int NB = SX > SY ? SX : SY;
+    static_assert(YSTAGE % 128 == 0, "y output staging must stay 128-byte aligned");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* base = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+    unsigned char* wb = base + (size_t)warp * WB;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)NW * WB) + warp * NB;
+    if (lane == 0) {
+        for (int s = 0; s < NB; ++s) mbar_init(smem_u32(&bar[s]), 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    uint32_t phase = 0;
+    const int total = e.total_x + e.total_y;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = (int)atomicAdd(&e.sched->next, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total) break;
+        if (t < e.total_x) {
+            const int q = ens_find(e.x_off, e.ninst, t);
+            const EnsInst<T>& I = e.inst[q];
+            Ctl* ctl = I.xa.ctl;
+            if (!__ldcg(&ctl->done)) {
+                const int cur = __ldcg(&ctl->cur);
+                const bool to = x_task<T, S, SX, true>(&I.tm_x[cur], &I.tm_xo, I.xa, t - e.x_off[q],
+                                                       reinterpret_cast<T*>(wb), bar, phase, lane);
+                if (to && lane == 0) atomicOr(&ctl->status, (int)kStatusTimeout);
+            }
+            // publish this task's Utmp writes (TMA stores completed by the
+            // task's final bulk wait, ghost rows by plain stores)
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) {
+                fence_proxy_async_global();
+                __threadfence();
+                atomicAdd(&e.sched->xdone[q], 1u);
+            }
+        } else {
+            const int ty = t - e.total_x;
+            const int q = ens_find(e.y_off, e.ninst, ty);
+            const EnsInst<T>& I = e.inst[q];
+            Ctl* ctl = I.xa.ctl;
+            if (__ldcg(&ctl->done)) continue;
+            int ok = 1;
+            if (lane == 0) {
+                ok = wait_count_bounded(&e.sched->xdone[q], (unsigned)I.xa.ntasks) ? 1 : 0;
+                fence_proxy_async_global();
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            const int cur = __ldcg(&ctl->cur);
+            const SweepArgs<T>& a = I.ya[1 - cur];
+            YOut<T> o{T(0), false, true};
+            if (ok)
+                o = y_task<T, S, RY, BWY, SY, true>(&I.tm_y, &I.tm_yo[1 - cur], a, ty - e.y_off[q],
+                                                     reinterpret_cast<T*>(wb),
+                                                     reinterpret_cast<T*>(wb + SY * YSTAGE), bar, phase, lane);
+            warp_arrive<T>(ctl, o.smax, o.bad, o.timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);
+        }
+    }
+}
+
+// Dynamic shared memory of the ensemble kernel.
+template <class T, int SX, int RY, int BWY, int SY, int NW> constexpr size_t ensemble_smem() {
+    constexpr int CX = 32 / sizeof(T);
+    constexpr size_t XB = (size_t)SX * 4 * 32 * CX * sizeof(T);
+    constexpr size_t YB = SY * (size_t)4 * RY * BWY * sizeof(T) + 2 * (size_t)4 * RY * 32 * sizeof(T);
+    constexpr size_t WB = ((XB > YB ? XB : YB) + 1023) / 1024 * 1024;
+    constexpr int NB = SX > SY ? SX : SY;
+    return 1024 + NW * WB + NW * NB * sizeof(uint64_t);
 }
 
 // ---------------------------------------------------------------------------

@@ -98,6 +98,24 @@ __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.
 // Wait until every committed bulk store has completed.
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// Order this thread's generic-proxy global accesses with async-proxy (TMA)
+// accesses to global memory (producer/consumer hand-offs between CTAs).
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Bounded acquire-spin until *p >= target.  Returns false on time-out.
+__device__ __forceinline__ bool wait_count_bounded(const unsigned int* p, unsigned int target) {
+    const unsigned long long t0 = globaltimer_ns();
+    for (uint32_t it = 0;; ++it) {
+        unsigned int v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        if (v >= target) return true;
+        if ((it & 63u) == 63u && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+        __nanosleep(64);
+    }
+}
+
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }

@@ -55,6 +55,8 @@ EXPORTS = (
     "eu_get_dt_log", "eu_set_device", "eu_set_option", "eu_get_option", "eu_read_planes",
     "eu_advance_first_order", "eu_advance_first_order_host", "eu_totals_noalloc",
     "eu_adjoint_forward", "eu_adjoint_backward", "eu_adjoint_timing", "eu_autotune",
+    "eu_batch_create", "eu_batch_destroy", "eu_batch_last_error", "eu_batch_handle", "eu_batch_start",
+    "eu_batch_step", "eu_batch_run", "eu_batch_time_steps", "eu_batch_autotune",
 )
 
 _lib = None
@@ -118,6 +120,19 @@ def load(path: str = LIB_PATH):
     L.eu_adjoint_backward.argtypes = [H, _dp, _dp]
     L.eu_adjoint_timing.argtypes = [H, C.POINTER(C.c_float)]
     L.eu_autotune.argtypes = [H, C.c_int, C.POINTER(C.c_longlong)]
+    B = C.c_void_p
+    L.eu_batch_create.argtypes = [C.c_int, C.POINTER(EuCase), C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(B)]
+    L.eu_batch_destroy.argtypes = [B]
+    L.eu_batch_destroy.restype = None
+    L.eu_batch_last_error.argtypes = [B]
+    L.eu_batch_last_error.restype = C.c_char_p
+    L.eu_batch_handle.argtypes = [B, C.c_int]
+    L.eu_batch_handle.restype = C.c_void_p
+    L.eu_batch_start.argtypes = [B]
+    L.eu_batch_step.argtypes = [B, C.c_longlong, C.POINTER(C.c_int)]
+    L.eu_batch_run.argtypes = [B, C.c_longlong, C.POINTER(C.c_longlong)]
+    L.eu_batch_time_steps.argtypes = [B, C.c_int, C.POINTER(C.c_float)]
+    L.eu_batch_autotune.argtypes = [B, C.c_int, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -196,6 +211,17 @@ class Solver:
         self.shape = (cfg.ny + 4, cfg.nx + 4, 4)
 
     @classmethod
+    def _view(cls, L, h, cfg, precision, solver, bc):
+        """A non-owning Solver over a handle owned by a Batch."""
+        s = cls.__new__(cls)
+        s.cfg, s.precision, s.solver, s.bc = cfg, precision, solver, tuple(bc)
+        s._h = C.c_void_p(h)
+        s._L = L
+        s.shape = (cfg.ny + 4, cfg.nx + 4, 4)
+        s._owned = False
+        return s
+
+    @classmethod
     def for_problem(cls, prob: Problem, precision="fp64", solver="hllc"):
         s = cls(prob.cfg, precision, solver, prob.bc)
         s.init(prob)
@@ -203,7 +229,8 @@ class Solver:
 
     def close(self):
         if getattr(self, "_h", None):
-            self._L.eu_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._L.eu_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -380,3 +407,75 @@ class Solver:
         ms = (C.c_float * 3)()
         self._check(self._L.eu_time_steps(self._h, int(nsteps), int(bool(use_graph)), ms))
         return float(ms[0]), float(ms[1]), float(ms[2])
+
+
+class Batch:
+    """An uneven ensemble: one grid per Problem (own size, boundaries,
+    parameters, CFL, t_end and dt), advanced by one persistent launch per
+    step.  ``instances[i]`` is a non-owning Solver view of instance i."""
+
+    def __init__(self, problems, precision="fp32", solver="hllc"):
+        L = load()
+        n = len(problems)
+        cases = (EuCase * n)(*[EuCase(p.cfg.nx, p.cfg.ny, p.cfg.ng, p.cfg.x_min, p.cfg.x_max, p.cfg.y_min,
+                                      p.cfg.y_max, p.cfg.cfl, p.cfg.t_end) for p in problems])
+        bcs = (C.c_int * (4 * n))(*[int(b) for p in problems for b in p.bc])
+        prec = FP32 if precision in ("fp32", FP32) else FP64
+        sid = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        b = C.c_void_p()
+        rc = L.eu_batch_create(n, cases, bcs, prec, sid, C.byref(b))
+        if rc:
+            raise EulerError(rc, L.eu_batch_last_error(None).decode())
+        self._b, self._L, self.problems = b, L, list(problems)
+        self.instances = [Solver._view(L, L.eu_batch_handle(b, i), p.cfg, precision, solver, p.bc)
+                          for i, p in enumerate(problems)]
+        for inst, p in zip(self.instances, problems):
+            inst.init(p)
+
+    def _check(self, rc):
+        if rc:
+            raise EulerError(rc, self._L.eu_batch_last_error(self._b).decode())
+
+    @property
+    def cells(self) -> int:
+        return sum(p.cfg.nx * p.cfg.ny for p in self.problems)
+
+    def start(self):
+        self._check(self._L.eu_batch_start(self._b))
+
+    def step(self, nsteps: int) -> bool:
+        done = C.c_int()
+        self._check(self._L.eu_batch_step(self._b, int(nsteps), C.byref(done)))
+        return bool(done.value)
+
+    def run(self, max_steps: int = 1 << 40) -> int:
+        n = C.c_longlong()
+        self._check(self._L.eu_batch_run(self._b, int(max_steps), C.byref(n)))
+        return n.value
+
+    def time_steps(self, nsteps: int) -> float:
+        ms = C.c_float()
+        self._check(self._L.eu_batch_time_steps(self._b, int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def autotune(self, steps: int = 4):
+        out = (C.c_longlong * 2)()
+        self._check(self._L.eu_batch_autotune(self._b, int(steps), out))
+        return int(out[0]), int(out[1])
+
+    def close(self):
+        if getattr(self, "_b", None):
+            for v in self.instances:
+                v._h = None
+            self._L.eu_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+

@@ -1,0 +1,82 @@
+"""Uneven ensembles (eu_batch_*): many grids with their own sizes,
+boundaries, parameters, CFL and t_end advanced by one persistent launch per
+step.  Each instance must reproduce, bit for bit, the run of its own handle
+(same step count, same dt sequence, same final state)."""
+import numpy as np
+import pytest
+
+from large_sys_eq_opt_gb300.cases import (REFLECTIVE, TRANSMISSIVE, BlastParams, CaseConfig, Problem,
+                                          ShockBubbleParams)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def E():
+    import large_sys_eq_opt_gb300.euler2d as E
+    E.load()
+    return E
+
+
+def small_ensemble():
+    bub = (TRANSMISSIVE, TRANSMISSIVE, REFLECTIVE, REFLECTIVE)
+    return [
+        Problem(CaseConfig(64, 64, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.1), "blast", BlastParams(r=0.3, p_in=5.0)),
+        Problem(CaseConfig(96, 80, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.08), "blast", BlastParams(r=0.45, p_in=30.0)),
+        Problem(CaseConfig(37, 53, 2, 0.0, 2.0, 0.0, 2.0, 0.5, 0.05), "blast", BlastParams(r=0.25, p_in=2.0)),
+        Problem(CaseConfig(200, 79, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.02), "shock_bubble",
+                ShockBubbleParams(mach=1.6, rho_bubble=2.0), bc=bub),
+        Problem(CaseConfig(150, 59, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.03), "shock_bubble",
+                ShockBubbleParams(mach=1.15, rho_bubble=0.2), bc=bub),
+        Problem(CaseConfig(1, 40, 2, 0.0, 1.0, 0.0, 2.0, 0.8, 0.05), "blast", BlastParams(cx=0.5, r=0.5)),
+    ]
+
+
+@pytest.mark.parametrize("prec,solver", [("fp32", "hllc"), ("fp64", "hllc"), ("fp32", "exact"),
+                                         ("fp32", "force"), ("fp64", "hll")])
+def test_ensemble_matches_single_runs(E, prec, solver):
+    probs = small_ensemble()
+    with E.Batch(probs, prec, solver) as b:
+        b.start()
+        b.run()
+        got = [inst.download() for inst in b.instances]
+        times = [inst.time() for inst in b.instances]
+    for p, g, (t, n, _) in zip(probs, got, times):
+        with E.Solver.for_problem(p, prec, solver) as s:
+            info = s.run(p.cfg.t_end)
+            ref = s.download()
+        assert n == info["steps"], p
+        assert t == info["t"], p
+        assert np.array_equal(g, ref), p
+
+
+def test_ensemble_autotune_keeps_results(E):
+    probs = small_ensemble()
+    with E.Batch(probs, "fp32", "hllc") as a, E.Batch(probs, "fp32", "hllc") as b:
+        a.start()
+        b.start()
+        sx, sy = b.autotune(2)
+        assert sx % 8 == 0 and sy % 4 == 0
+        a.step(25)
+        b.step(25)
+        for u, v in zip(a.instances, b.instances):
+            assert np.array_equal(u.download(), v.download())
+
+
+def test_ensemble_workload_builds_and_steps(E):
+    """The 64-instance benchmark ensemble (48 blasts, 16 shock-bubbles)
+    steps, and a few instances match their own handles after 6 steps."""
+    from large_sys_eq_opt_gb300.cases import ensemble_problems
+    probs = ensemble_problems()
+    with E.Batch(probs, "fp32", "hllc") as b:
+        b.start()
+        done = b.step(6)
+        assert not done
+        picks = [0, 7, 47, 48, 63]
+        got = {i: b.instances[i].download() for i in picks}
+    # six CFL steps end far before any instance's t_end, so the unclipped
+    # eu_step_n of the instance's own handle is the reference
+    for i in picks:
+        with E.Solver.for_problem(probs[i], "fp32", "hllc") as s:
+            s.step_n(6)
+            assert np.array_equal(got[i], s.download()), probs[i].name

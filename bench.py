@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--skip-ensemble", action="store_true")
     return ap.parse_args()
 
 
@@ -272,6 +273,32 @@ def adjoint_leg(E, np):
     return res
 
 
+def ensemble_leg(E, np, steps=20):
+    """Uneven ensemble workload (48 blasts on {128..1024}^2, 16 shock-bubbles
+    500x198..2000x792, FP32 HLLC, per-instance CFL dt): one persistent launch
+    per step after the ensemble autotuner, against the same instances stepped
+    one after another on their own handles (each with its own tuned shape
+    and graph)."""
+    from large_sys_eq_opt_gb300.cases import ensemble_problems
+    probs = ensemble_problems()
+    with E.Batch(probs, "fp32", "hllc") as b:
+        b.start()
+        shape = b.autotune(3)
+        b.time_steps(3)
+        ms = b.time_steps(steps)
+        cells = b.cells
+    seq_ms = 0.0
+    for p in probs:
+        with E.Solver.for_problem(p, "fp32", "hllc") as s:
+            s.autotune(3)
+            s.time_steps(3)
+            seq_ms += s.time_steps(steps)[0]
+    return {"workload": f"ensemble_{len(probs)}_fp32_hllc", "instances": len(probs), "cells": cells,
+            "steps": steps, "seg_xy": list(shape), "ms_per_step": ms / steps,
+            "value": cells * steps / (ms / 1e3), "unit": UNIT,
+            "sequential_ms_per_step": seq_ms / steps, "speedup_vs_sequential": seq_ms / ms}
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -360,6 +387,10 @@ def run_ours(args, dist: Dist):
     # ---- discrete adjoint: time ratio against the forward -----------------
     if not args.skip_adjoint:
         out["adjoint"] = adjoint_leg(E, np)
+
+    # ---- uneven ensemble in one persistent launch per step ---------------
+    if not args.skip_ensemble:
+        out["ensemble"] = ensemble_leg(E, np)
 
     # ---- CPU baseline (oracle port on the host cores) ---------------------
     if dist.rank == 0 and dist.ws == 1 and not args.skip_cpu:

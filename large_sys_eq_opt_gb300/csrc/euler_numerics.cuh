@@ -641,22 +641,26 @@ template <class T> struct CellOut {
     bool r_phys;   // R.V is physical (the next cell's fast Riemann needs it)
 };
 
+// full = true: the cell's reconstruction flagged a fallback -- recompute
+// its primitives, face states and flux with the full logic.  full = false:
+// only the face flagged one -- keep the fast-path primitives and face states
+// (W, L, R) and recompute the flux.
 template <class T, int S>
-__device__ __noinline__ CellOut<T> cell_full(Cons<T> U, Prim<T> Wm2, Prim<T> Wm1, Face<T> Rp, T hl) {
+__device__ __noinline__ CellOut<T> cell_full(Cons<T> U, Prim<T> Wm2, Prim<T> Wm1, Face<T> Rp, T hl, bool full,
+                                             Prim<T> W, Face<T> L, Face<T> R) {
     CellOut<T> o;
-    o.W = c2p_cell(U);
-    reconstruct(Wm2, Wm1, o.W, hl, o.L, o.R);
+    if (full) {
+        o.W = c2p_cell(U);
+        reconstruct(Wm2, Wm1, o.W, hl, o.L, o.R);
+        o.r_phys = physical_riemann(o.R.V);
+    } else {
+        o.W = W;
+        o.L = L;
+        o.R = R;
+        o.r_phys = true;
+    }
     o.F = riemann<S>(Rp.U, Rp.V, o.L.U, o.L.V);
-    o.r_phys = physical_riemann(o.R.V);
     return o;
-}
-
-// Full-logic flux of one face whose right state came from the fast path
-// (taken when only the face flagged a fallback, e.g. a non-physical left
-// state).
-template <class T, int S>
-__device__ __noinline__ Cons<T> face_full(Face<T> Rp, Face<T> L) {
-    return riemann<S>(Rp.U, Rp.V, L.U, L.V);
 }
 
 // Largest signal speed max(|un|+a, |ut|+a) of a conserved state

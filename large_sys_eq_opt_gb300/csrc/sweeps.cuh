@@ -68,13 +68,9 @@ template <class T, int S> struct Line {
         Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow_face);
         bool r_phys = true;
         if (__builtin_expect(slow_cell | slow_face, 0)) {
-            if (slow_cell) {
-                const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl);
-                W = o.W; L = o.L; R = o.R; F = o.F;
-                r_phys = o.r_phys;
-            } else {
-                F = face_full<T, S>(Rp, L);
-            }
+            const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl, slow_cell, W, L, R);
+            W = o.W; L = o.L; R = o.R; F = o.F;
+            r_phys = o.r_phys;
         }
         const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
         A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};

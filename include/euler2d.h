@@ -214,6 +214,13 @@ int eu_batch_time_steps(eu_batch* b, int nsteps, float* ms);
  * (clipped to each grid), chosen by timing whole ensemble steps; states
  * restored afterwards. */
 int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]);
+/* Batched discrete adjoint: eu_adjoint_forward / eu_adjoint_backward of
+ * every instance (instance i: nsteps[i] steps with its own frozen dts[i]),
+ * enqueued on the instances' own streams so that they run concurrently.
+ * Gradients with respect to scalar case parameters follow by the chain
+ * rule dJ/dtheta = <dJ/dU_0, dU_0/dtheta> (large_sys_eq_opt_gb300/adjoint.py). */
+int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k);
+int eu_batch_adjoint_backward(eu_batch* b, const double* const* dJ_dUN, double* const* dJ_dU0);
 
 /* ---- drop-in calls on host grids (what the reference's callers pass) ------- */
 /* compute_dt(const Grid2D&, double): upload, reduce, read back dt. */

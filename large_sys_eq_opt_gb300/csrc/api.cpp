@@ -115,6 +115,8 @@ struct eu_handle {
         int hctl_cap = 0;
         int ring_seg = -1;
         bool ready = false;
+        double t0 = 0.0;
+        long long step0 = 0;
         cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
         float ms_fwd = 0.f, ms_bwd = 0.f;
     } adj;
@@ -600,6 +602,89 @@ cudaError_t adj_step(eu_handle* h, int s, int j) {
     x.lam_d = A.dts[n] / h->dx;
     x.bc_lo = h->bc[EU_SIDE_LEFT]; x.bc_hi = h->bc[EU_SIDE_RIGHT];
     return L(0, x, h->st);
+}
+
+// Enqueue the checkpointed forward on the handle's stream (no host wait).
+int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (nsteps < 1 || !dts) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: need nsteps >= 1 and a dt list");
+    if (ckpt_k < 1 || ckpt_k > 1024) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: ckpt_k must be in [1, 1024]");
+    if (h->cfg.nx < 2 || h->cfg.ny < 2) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: the adjoint needs nx, ny >= 2");
+    for (long long i = 0; i < nsteps; ++i)
+        if (!(dts[i] > 0.0) || !(dts[i] < INFINITY))
+            return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: every dt must be positive and finite");
+    auto& A = h->adj;
+    A.ready = false;
+    if (int rc = adj_prepare(h, nsteps, ckpt_k)) return rc;
+    A.dts.assign(dts, dts + nsteps);
+    A.t0 = h->hctl->t;
+    A.step0 = h->hctl->step;
+    EU_CUDA(h, cudaMemcpyAsync(A.d_dts, A.dts.data(), sizeof(double) * (size_t)nsteps, cudaMemcpyHostToDevice, h->st));
+    EU_CUDA(h, fill_ghosts(h, h->cur));   // scripts/cpu/main_cpu.cpp:222
+    EU_CUDA(h, cudaMemcpyAsync(A.ck[0], h->S[h->cur], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+    EU_CUDA(h, cudaEventRecord(A.ev[0], h->st));
+    for (int s = 0; s < A.nseg; ++s) EU_CUDA(h, adj_segment(h, s));
+    EU_CUDA(h, cudaEventRecord(A.ev[1], h->st));
+    A.ring_seg = A.nseg - 1;
+    EU_CUDA(h, cudaMemcpyAsync(h->S[h->cur], A.ck[A.nseg], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+    EU_CUDA(h, cudaMemcpyAsync(&A.hctl[A.nseg], h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    return EU_OK;
+}
+
+// Wait for the forward; status, timing, the handle's time and step.
+int adj_fwd_finish(eu_handle* h) {
+    auto& A = h->adj;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    EU_CUDA(h, cudaEventElapsedTime(&A.ms_fwd, A.ev[0], A.ev[1]));
+    const Ctl probe = A.hctl[A.nseg];
+    double t = A.t0;
+    for (double d : A.dts) t += d;
+    ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
+    h->hctl->t = t;
+    h->hctl->step = A.step0 + A.nsteps;
+    if (int rc = ctl_push(h)) return rc;
+    if (probe.status & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
+    if (probe.status & kStatusNonFinite) return fail(h, EU_ERR_NONPHYSICAL, "non-finite state in the forward steps");
+    A.ready = true;
+    return EU_OK;
+}
+
+int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (!dJ_dUN || !dJ_dU0) return fail(h, EU_ERR_INVALID, "eu_adjoint_backward: null argument");
+    auto& A = h->adj;
+    if (!A.ready) return fail(h, EU_ERR_STATE, "eu_adjoint_backward: call eu_adjoint_forward first");
+    if (int rc = ensure_aos(h)) return rc;
+    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, dJ_dUN, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
+    if (h->prec == EU_FP32) EU_CUDA(h, launch_pack_aos<float>(h->d_aos, Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
+    else EU_CUDA(h, launch_pack_aos<double>(h->d_aos, Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
+    EU_CUDA(h, cudaEventRecord(A.ev[2], h->st));
+    for (int s = A.nseg - 1; s >= 0; --s) {
+        if (A.ring_seg != s) {
+            EU_CUDA(h, adj_segment(h, s));
+            A.ring_seg = s;
+        }
+        const int len = (int)std::min<long long>(A.k, A.nsteps - (long long)s * A.k);
+        for (int j = len - 1; j >= 0; --j) EU_CUDA(h, adj_step(h, s, j));
+    }
+    EU_CUDA(h, cudaEventRecord(A.ev[3], h->st));
+    const int bcz[4] = {0, 0, 0, 0};
+    if (h->prec == EU_FP32) EU_CUDA(h, launch_unpack_aos<float>(Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
+    else EU_CUDA(h, launch_unpack_aos<double>(Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
+    EU_CUDA(h, cudaMemcpyAsync(dJ_dU0, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
+    return EU_OK;
+}
+
+int adj_bwd_finish(eu_handle* h, double* dJ_dU0) {
+    auto& A = h->adj;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    EU_CUDA(h, cudaEventElapsedTime(&A.ms_bwd, A.ev[2], A.ev[3]));
+    // the gradient is with respect to the interior; ghost entries are zero
+    const int tnx = h->cfg.nx + 4, tny = h->cfg.ny + 4;
+    for (int j = 0; j < tny; ++j)
+        for (int i = 0; i < tnx; ++i)
+            if (i < 2 || i >= tnx - 2 || j < 2 || j >= tny - 2) std::memset(dJ_dU0 + 4 * ((size_t)j * tnx + i), 0, 32);
+    return EU_OK;
 }
 
 template <class T> Planes<T> planes_of(const eu_handle* h, void* b) {
@@ -1093,75 +1178,13 @@ int eu_totals(eu_handle* h, double out[4]) {
 // --- drop-in calls on host grids -----------------------------------------------
 // --- discrete adjoint -----------------------------------------------------------
 int eu_adjoint_forward(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
-    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
-    if (nsteps < 1 || !dts) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: need nsteps >= 1 and a dt list");
-    if (ckpt_k < 1 || ckpt_k > 1024) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: ckpt_k must be in [1, 1024]");
-    if (h->cfg.nx < 2 || h->cfg.ny < 2) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: the adjoint needs nx, ny >= 2");
-    for (long long i = 0; i < nsteps; ++i)
-        if (!(dts[i] > 0.0) || !(dts[i] < INFINITY))
-            return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: every dt must be positive and finite");
-    auto& A = h->adj;
-    A.ready = false;
-    if (int rc = adj_prepare(h, nsteps, ckpt_k)) return rc;
-    A.dts.assign(dts, dts + nsteps);
-    EU_CUDA(h, cudaMemcpyAsync(A.d_dts, A.dts.data(), sizeof(double) * (size_t)nsteps, cudaMemcpyHostToDevice, h->st));
-    const double t0 = h->hctl->t;
-    const long long step0 = h->hctl->step;
-    EU_CUDA(h, fill_ghosts(h, h->cur));   // scripts/cpu/main_cpu.cpp:222
-    EU_CUDA(h, cudaMemcpyAsync(A.ck[0], h->S[h->cur], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
-    EU_CUDA(h, cudaEventRecord(A.ev[0], h->st));
-    for (int s = 0; s < A.nseg; ++s) EU_CUDA(h, adj_segment(h, s));
-    EU_CUDA(h, cudaEventRecord(A.ev[1], h->st));
-    A.ring_seg = A.nseg - 1;
-    EU_CUDA(h, cudaMemcpyAsync(h->S[h->cur], A.ck[A.nseg], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
-    // status of the segment launches, then the handle's own control block
-    Ctl& probe = A.hctl[A.nseg];
-    EU_CUDA(h, cudaMemcpyAsync(&probe, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
-    EU_CUDA(h, cudaStreamSynchronize(h->st));
-    EU_CUDA(h, cudaEventElapsedTime(&A.ms_fwd, A.ev[0], A.ev[1]));
-    double t = t0;
-    for (double d : A.dts) t += d;
-    ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
-    h->hctl->t = t;
-    h->hctl->step = step0 + nsteps;
-    if (int rc = ctl_push(h)) return rc;
-    if (probe.status & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
-    if (probe.status & kStatusNonFinite) return fail(h, EU_ERR_NONPHYSICAL, "non-finite state in the forward steps");
-    A.ready = true;
-    return EU_OK;
+    if (int rc = adj_fwd_enqueue(h, nsteps, dts, ckpt_k)) return rc;
+    return adj_fwd_finish(h);
 }
 
 int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
-    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
-    if (!dJ_dUN || !dJ_dU0) return fail(h, EU_ERR_INVALID, "eu_adjoint_backward: null argument");
-    auto& A = h->adj;
-    if (!A.ready) return fail(h, EU_ERR_STATE, "eu_adjoint_backward: call eu_adjoint_forward first");
-    if (int rc = ensure_aos(h)) return rc;
-    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, dJ_dUN, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
-    if (h->prec == EU_FP32) EU_CUDA(h, launch_pack_aos<float>(h->d_aos, planes_of<float>(h, A.lam), h->cfg.nx, h->cfg.ny, h->st));
-    else EU_CUDA(h, launch_pack_aos<double>(h->d_aos, planes_of<double>(h, A.lam), h->cfg.nx, h->cfg.ny, h->st));
-    EU_CUDA(h, cudaEventRecord(A.ev[2], h->st));
-    for (int s = A.nseg - 1; s >= 0; --s) {
-        if (A.ring_seg != s) {
-            EU_CUDA(h, adj_segment(h, s));
-            A.ring_seg = s;
-        }
-        const int len = (int)std::min<long long>(A.k, A.nsteps - (long long)s * A.k);
-        for (int j = len - 1; j >= 0; --j) EU_CUDA(h, adj_step(h, s, j));
-    }
-    EU_CUDA(h, cudaEventRecord(A.ev[3], h->st));
-    const int bcz[4] = {0, 0, 0, 0};
-    if (h->prec == EU_FP32) EU_CUDA(h, launch_unpack_aos<float>(planes_of<float>(h, A.lam), kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
-    else EU_CUDA(h, launch_unpack_aos<double>(planes_of<double>(h, A.lam), kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
-    EU_CUDA(h, cudaMemcpyAsync(dJ_dU0, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
-    EU_CUDA(h, cudaStreamSynchronize(h->st));
-    EU_CUDA(h, cudaEventElapsedTime(&A.ms_bwd, A.ev[2], A.ev[3]));
-    // the gradient is with respect to the interior; ghost entries are zero
-    const int tnx = h->cfg.nx + 4, tny = h->cfg.ny + 4;
-    for (int j = 0; j < tny; ++j)
-        for (int i = 0; i < tnx; ++i)
-            if (i < 2 || i >= tnx - 2 || j < 2 || j >= tny - 2) std::memset(dJ_dU0 + 4 * ((size_t)j * tnx + i), 0, 32);
-    return EU_OK;
+    if (int rc = adj_bwd_enqueue(h, dJ_dUN, dJ_dU0)) return rc;
+    return adj_bwd_finish(h, dJ_dU0);
 }
 
 int eu_adjoint_timing(eu_handle* h, float ms[2]) {
@@ -1628,6 +1651,31 @@ int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]) {
     b->dirty = true;
     if (rc != EU_OK) return rc;
     if (chosen) { chosen[0] = bx; chosen[1] = by; }
+    return EU_OK;
+}
+
+// Adjoints of every instance, enqueued on the instances' own streams so that
+// they run concurrently, then awaited.
+int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k) {
+    if (!b || !nsteps || !dts) return bfail(b, EU_ERR_INVALID, "bad argument");
+    if (cudaStreamSynchronize(b->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "batch stream failed");
+    for (int i = 0; i < b->n; ++i)
+        if (int rc = adj_fwd_enqueue(b->h[(size_t)i], nsteps[i], dts[i], ckpt_k))
+            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+    for (int i = 0; i < b->n; ++i)
+        if (int rc = adj_fwd_finish(b->h[(size_t)i]))
+            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+    return EU_OK;
+}
+
+int eu_batch_adjoint_backward(eu_batch* b, const double* const* dJ_dUN, double* const* dJ_dU0) {
+    if (!b || !dJ_dUN || !dJ_dU0) return bfail(b, EU_ERR_INVALID, "bad argument");
+    for (int i = 0; i < b->n; ++i)
+        if (int rc = adj_bwd_enqueue(b->h[(size_t)i], dJ_dUN[i], dJ_dU0[i]))
+            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+    for (int i = 0; i < b->n; ++i)
+        if (int rc = adj_bwd_finish(b->h[(size_t)i], dJ_dU0[i]))
+            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
     return EU_OK;
 }
 

@@ -57,6 +57,7 @@ EXPORTS = (
     "eu_adjoint_forward", "eu_adjoint_backward", "eu_adjoint_timing", "eu_autotune",
     "eu_batch_create", "eu_batch_destroy", "eu_batch_last_error", "eu_batch_handle", "eu_batch_start",
     "eu_batch_step", "eu_batch_run", "eu_batch_time_steps", "eu_batch_autotune",
+    "eu_batch_adjoint_forward", "eu_batch_adjoint_backward",
 )
 
 _lib = None
@@ -133,6 +134,8 @@ def load(path: str = LIB_PATH):
     L.eu_batch_run.argtypes = [B, C.c_longlong, C.POINTER(C.c_longlong)]
     L.eu_batch_time_steps.argtypes = [B, C.c_int, C.POINTER(C.c_float)]
     L.eu_batch_autotune.argtypes = [B, C.c_int, C.POINTER(C.c_longlong)]
+    L.eu_batch_adjoint_forward.argtypes = [B, C.POINTER(C.c_longlong), C.POINTER(_dp), C.c_int]
+    L.eu_batch_adjoint_backward.argtypes = [B, C.POINTER(_dp), C.POINTER(_dp)]
     _lib = L
     return L
 
@@ -462,6 +465,25 @@ class Batch:
         out = (C.c_longlong * 2)()
         self._check(self._L.eu_batch_autotune(self._b, int(steps), out))
         return int(out[0]), int(out[1])
+
+    def adjoint_forward(self, dts_list, ckpt_k: int = 32):
+        """Checkpointed forward of every instance with its own frozen dts."""
+        n = len(self.instances)
+        arrs = [np.ascontiguousarray(d, dtype=np.float64) for d in dts_list]
+        ns = (C.c_longlong * n)(*[len(a) for a in arrs])
+        ptrs = (_dp * n)(*[_p(a) for a in arrs])
+        self._keep = arrs
+        self._check(self._L.eu_batch_adjoint_forward(self._b, ns, ptrs, int(ckpt_k)))
+
+    def adjoint_backward(self, grads_N):
+        """dJ/dU_0 of every instance from its dJ/dU_N (concurrently)."""
+        n = len(self.instances)
+        ins = [np.ascontiguousarray(g, dtype=np.float64) for g in grads_N]
+        outs = [np.zeros(v.shape) for v in self.instances]
+        pin = (_dp * n)(*[_p(a) for a in ins])
+        pout = (_dp * n)(*[_p(a) for a in outs])
+        self._check(self._L.eu_batch_adjoint_backward(self._b, pin, pout))
+        return outs
 
     def close(self):
         if getattr(self, "_b", None):

@@ -80,3 +80,36 @@ def test_ensemble_workload_builds_and_steps(E):
         with E.Solver.for_problem(probs[i], "fp32", "hllc") as s:
             s.step_n(6)
             assert np.array_equal(got[i], s.download()), probs[i].name
+
+
+def test_batched_parameter_gradients_match_fd(E):
+    """dJ/dtheta of every instance of a small mixed batch (FP64) through the
+    batched adjoint, against central differences of J(theta +- eps) run on
+    the instance's own handle with the same frozen dts."""
+    from large_sys_eq_opt_gb300 import adjoint as A
+    bub = (TRANSMISSIVE, TRANSMISSIVE, REFLECTIVE, REFLECTIVE)
+    probs = [
+        Problem(CaseConfig(48, 48, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.25), "blast", BlastParams(r=0.33, p_in=7.0)),
+        Problem(CaseConfig(64, 56, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.25), "blast", BlastParams(r=0.45, p_in=40.0)),
+        Problem(CaseConfig(120, 48, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.1), "shock_bubble",
+                ShockBubbleParams(mach=1.5, rho_bubble=2.2), bc=bub),
+        Problem(CaseConfig(150, 59, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.1), "shock_bubble",
+                ShockBubbleParams(mach=1.2, rho_bubble=0.3), bc=bub),
+    ]
+    Js, grads, dts, _ = A.ensemble_parameter_gradients(E, probs, 60, precision="fp64", solver="hllc", ckpt_k=16)
+    from dataclasses import replace
+    for p, J, g, d in zip(probs, Js, grads, dts):
+        mask = A.objective_mask(p)
+        with E.Solver(p.cfg, "fp64", "hllc", bc=p.bc) as s:
+            for name, val in g.items():
+                theta = getattr(p.params, name)
+                eps = 1e-6 * abs(theta)
+                J2 = []
+                for sgn in (1.0, -1.0):
+                    q = replace(p, params=replace(p.params, **{name: theta + sgn * eps}))
+                    s.upload(A.initial_state(q)[0])
+                    s.step_n(len(d), d)
+                    J2.append(A.objective(s.download(), mask))
+                fd = (J2[0] - J2[1]) / (2 * eps)
+                print(p.name or p.kind, name, "adjoint %.10e fd %.10e" % (val, fd))
+                assert abs(val - fd) <= 1e-5 * abs(fd) + 1e-9 * abs(J), (p, name, val, fd)

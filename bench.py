@@ -48,7 +48,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
-    ap.add_argument("--n", type=int, default=8192, help="grid is n x n")
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=8192, help="grid is n x n")
     ap.add_argument("--solver", default="hllc", choices=("hll", "hllc", "exact", "force"))
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")

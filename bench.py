@@ -273,6 +273,48 @@ def adjoint_leg(E, np):
     return res
 
 
+FIELDS = ("rho", "rhou", "rhov", "E", "p")
+
+
+def field_errors(np, got, ref):
+    """Per-field L1 (mean absolute) and Linf differences over the interior."""
+    def fields(A):
+        r, mu, mv, en = (A[2:-2, 2:-2, k] for k in range(4))
+        return (r, mu, mv, en, 0.3999999999999999 * (en - 0.5 * (mu * mu + mv * mv) / r))
+    out = {}
+    for name, a, b in zip(FIELDS, fields(got), fields(ref)):
+        d = np.abs(a - b)
+        out[name] = {"l1": float(d.mean()), "linf": float(d.max())}
+    return out
+
+
+def fp32_error_leg(E, np):
+    """FP32 form against FP64 per field and per configuration, both on the
+    FP64 run's dt sequence: the 256^2 blast and the 1000x396 reflective
+    shock-bubble to t_end (HLLC), the 512^2 adjoint case (400 steps)."""
+    from large_sys_eq_opt_gb300.cases import blast_256, blast_adjoint_512, shock_bubble_1000x396
+    res = {}
+    for name, prob, nsteps in (("config0_blast256_t_end", blast_256(), None),
+                               ("config1_shock_bubble_1000x396_t_end", shock_bubble_1000x396(), None),
+                               ("config3_blast512_400steps", blast_adjoint_512(), 400)):
+        s64 = E.Solver.for_problem(prob, "fp64", "hllc")
+        s64.set_dt_log(1 << 16)
+        if nsteps is None:
+            info = s64.run(prob.cfg.t_end)
+            nsteps = info["steps"]
+        else:
+            s64.step_n(nsteps)
+        dts = s64.dt_log(nsteps)
+        ref = s64.download()
+        s64.close()
+        s32 = E.Solver.for_problem(prob, "fp32", "hllc")
+        s32.step_n(nsteps, dts)
+        got = s32.download()
+        s32.close()
+        res[name] = {"steps": int(nsteps), **field_errors(np, got, ref)}
+    return res
+
+
 def ensemble_leg(E, np, steps=20):
     """Uneven ensemble workload (48 blasts on {128..1024}^2, 16 shock-bubbles
     500x198..2000x792, FP32 HLLC, per-instance CFL dt): one persistent launch
@@ -386,11 +428,12 @@ def run_ours(args, dist: Dist):
 
         drho = np.abs(got[2:-2, 2:-2, 0] - ref[2:-2, 2:-2, 0])
         dp = np.abs(pres(got) - pres(ref))
+        per_field = field_errors(np, got, ref)
         out["fp64"] = {"value": v64, "ms_per_step": tot64 / K,
                        "per_kernel_ms": {"sweep_x": tx64 / K, "sweep_y": ty64 / K}}
         out["fp32_vs_fp64"] = {"speedup": value / v64, "steps": W + K, "dt": "FP64 dt sequence replayed",
                                "l1_rho": float(drho.mean()), "linf_rho": float(drho.max()),
-                               "l1_p": float(dp.mean()), "linf_p": float(dp.max())}
+                               "l1_p": float(dp.mean()), "linf_p": float(dp.max()), "per_field": per_field}
         del got, ref, drho, dp
 
     # ---- e2e through the drop-in call on host grids -----------------------
@@ -417,6 +460,10 @@ def run_ours(args, dist: Dist):
     # ---- discrete adjoint: time ratio against the forward -----------------
     if not args.skip_adjoint:
         out["adjoint"] = adjoint_leg(E, np)
+
+    # ---- FP32 error per field and configuration ----------------------------
+    if not args.skip_fp64:
+        out["fp32_error_by_config"] = fp32_error_leg(E, np)
 
     # ---- uneven ensemble in one persistent launch per step ---------------
     if not args.skip_ensemble:

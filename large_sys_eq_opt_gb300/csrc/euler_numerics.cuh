@@ -380,8 +380,11 @@ __device__ __forceinline__ Cons<T> riemann(const Cons<T>& UL, const Prim<T>& VL,
 // (src/cpu/solver_cpu.cpp:22-28); for same-sign arguments min(a,b) (a > 0)
 // or max(a,b) (a < 0) equals copysign(min(|a|,|b|), a) exactly.
 template <class T> __device__ __forceinline__ T minmod(T a, T b) {
-    const T m = copysign(Ar<T>::fmin_(Ar<T>::fabs_(a), Ar<T>::fabs_(b)), a);
-    return (a * b > T(0)) ? m : T(0);
+    // = max(0, min(a, b)) + min(0, max(a, b)): both terms vanish for
+    // arguments of opposite sign (or a zero), otherwise one of them is the
+    // argument nearer zero.  (The reference's test a*b > 0 also rejects
+    // same-sign pairs whose product underflows, below 1e-308 in FP64.)
+    return Ar<T>::fmax_(T(0), Ar<T>::fmin_(a, b)) + Ar<T>::fmin_(T(0), Ar<T>::fmax_(a, b));
 }
 
 // Face states of one cell: the half-step-evolved left/right boundary states
@@ -445,20 +448,30 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
 template <class T> __device__ __forceinline__ bool finite4(T a, T b, T c, T d) {
     return Ar<T>::fabs_((a + b) + (c + d)) < T(INFINITY);
 }
+// Physicality tests of primitives that came out of c2p_fast.  They need no
+// separate test of u_n and u_t: the pressure is E(g-1) - (g-1)/2 (m_n u_n +
+// m_t u_t), so a non-finite momentum or velocity (u = m / rho with rho above
+// the floor) makes p NaN or -inf, which fails p > floor, and NaN in rho or p
+// fails the comparisons.  A state with rho or E = +inf passes; it can only
+// come from a state that is already non-finite, whose step reports
+// EU_ERR_NONPHYSICAL through the y-sweep's finiteness check of its outputs.
+template <class T> __device__ __forceinline__ bool phys_above(const Prim<T>& V, T floor) {
+    return (V.r > floor) & (V.p > floor);
+}
 // physical_recon, with the 1e-12 floors (src/cpu/solver_cpu.cpp:39-43)
 template <class T> __device__ __forceinline__ bool phys_recon_fast(const Prim<T>& V) {
-    return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(kRhoFloorD);
+    return phys_above(V, T(kRhoFloorD));
 }
 // physical_riemann (head/riemann.hpp:74-81)
 template <class T> __device__ __forceinline__ bool phys_riemann_fast(const Prim<T>& V) {
-    return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(0);
+    return phys_above(V, T(0));
 }
 // A cell whose limited face states are physical for any minmod slope: with
 // finite neighbours of non-negative rho and p, minmod keeps the face values
 // of rho and p at or above half the centre value, so rho, p > 4e-12 leaves
 // them above the 1e-12 floors (src/cpu/solver_cpu.cpp:83-87).
 template <class T> __device__ __forceinline__ bool nice_cell(const Prim<T>& V) {
-    return finite4(V.r, V.un, V.ut, V.p) && Ar<T>::fmin_(V.r, V.p) > T(4.0e-12);
+    return phys_above(V, T(4.0e-12));
 }
 
 // cons_to_prim of a cell state, with the rounding fixed by explicit fused

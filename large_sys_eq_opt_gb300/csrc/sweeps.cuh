@@ -53,24 +53,51 @@ template <class T, int S> struct Line {
         rp_phys = false;
     }
 
+    // Start of a line at cell U0: the window as if U0 were repeated to the
+    // left (zero slopes, faces equal to the cell).  Only the first outputs'
+    // warm-up sees these values, and no output depends on them; they just
+    // keep the first pushes from raising fallback flags on garbage.
+    __device__ __forceinline__ void prime(const Cons<T>& U0) {
+        bool isl = false;
+        const Prim<T> W = c2p_fast(U0, isl);
+        Wm2 = W; Wm1 = W;
+        Um1 = U0;
+        A = U0;
+        Rp.U = U0;
+        Rp.V = W;
+        nice2 = nice1 = nice_cell(W);
+        rp_phys = phys_riemann_fast(W);
+    }
+
     // U(c-2) - lam (F(c-3/2) - F(c-5/2)) is evaluated as A - lam F(c-3/2)
     // (src/cpu/solver_cpu.cpp:452-453, :489-490).
-    // A cell flagged by its own reconstruction is recomputed in full; a cell
-    // whose only flag is the face (a non-physical left face state, a Riemann
-    // fallback) keeps its fast-path primitives and face states and
-    // recomputes only the flux.
-    __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
-        bool slow_cell = false, slow_face = !rp_phys;
-        Prim<T> W = c2p_fast(U, slow_cell);
+    // SLOW = true: a cell flagged by its own reconstruction is recomputed in
+    // full; a cell whose only flag is the face (a non-physical left face
+    // state, a Riemann fallback) keeps its fast-path primitives and face
+    // states and recomputes only the flux.
+    // SLOW = false: the fast path only; the flags are returned (fi: the
+    // cell's own FP64 pressure island, fc: its reconstruction, ff: its face)
+    // and the caller redoes the work with SLOW = true when one matters.
+    template <bool SLOW>
+    __device__ __forceinline__ Cons<T> step(const Cons<T>& U, T hl, T lam, bool& fi, bool& fc, bool& ff) {
+        bool isl = false, slow_cell = false, slow_face = !rp_phys;
+        Prim<T> W = c2p_fast(U, isl);
         const bool nice = nice_cell(W);
         Face<T> L, R;
         reconstruct_fast(Wm2, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell);
         Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow_face);
         bool r_phys = true;
-        if (__builtin_expect(slow_cell | slow_face, 0)) {
-            const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl, slow_cell, W, L, R);
-            W = o.W; L = o.L; R = o.R; F = o.F;
-            r_phys = o.r_phys;
+        if constexpr (SLOW) {
+            slow_cell |= isl;
+            if (__builtin_expect(slow_cell | slow_face, 0)) {
+                const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl, slow_cell, W, L, R);
+                W = o.W; L = o.L; R = o.R; F = o.F;
+                r_phys = o.r_phys;
+            }
+        } else {
+            fi |= isl;
+            fc |= slow_cell;
+            ff |= slow_face;
         }
         const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
         A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
@@ -80,6 +107,10 @@ template <class T, int S> struct Line {
         nice2 = nice1; nice1 = nice;
         rp_phys = r_phys;
         return N;
+    }
+    __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
+        bool a = false, b = false, c = false;
+        return step<true>(U, hl, lam, a, b, c);
     }
 };
 
@@ -437,10 +468,17 @@ template <class T> struct YOut {
     bool bad, timed_out;
 };
 
-// One y-sweep task (one warp): 32 S columns x one segment of rows.
-template <class T, int S, int RY, int BW, int STAGES, bool PERSIST>
-__device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
-                                          int task, T* buf, T* obuf, uint64_t* bar, uint32_t& phase, int lane) {
+// One pass of a y-sweep task (one warp): 32 S columns x one segment of rows.
+// FAST = true runs the fast path only and gives up (aborted = true, nothing
+// of the box in hand stored, boxes in flight drained) as soon as any lane
+// flags a fallback that can reach an output; the caller then reruns the
+// task with FAST = false, whose push handles every fallback.  Keeping the
+// out-of-line fallback call out of the hot loop is worth about a third of
+// the y-sweep's time; outputs do not depend on which pass produced them.
+template <class T, int S, int RY, int BW, int STAGES, bool FAST>
+__device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
+                                          int task, T* buf, T* obuf, uint64_t* bar, uint32_t& phase, int lane,
+                                          bool& aborted) {
     constexpr int STAGE = 4 * RY * BW;
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
     constexpr int OSTAGE = 4 * RY * 32;          // output box: 4 fields x RY rows x 32 columns
@@ -463,6 +501,7 @@ __device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorM
     const double lam_d = __ldcg(&ctl->dt) / a.d; // dt/dy
     const T lam = T(lam_d);
     const T hl = T(0.5 * lam_d);
+    aborted = false;
 
     if (lane == 0) {
         tma_prefetch_desc(tm);
@@ -488,7 +527,7 @@ __device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorM
     int kfail = nst;
     for (int k = 0; k < nst; ++k) {
         const int s = k % STAGES;
-        if (!stage_wait<PERSIST>(bar, s, k, STAGES, phase)) {
+        if (!stage_wait<true>(bar, s, k, STAGES, phase)) {
             timed_out = true;
             kfail = k;
             break;
@@ -499,11 +538,24 @@ __device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorM
         __syncwarp();
         const int ir0 = r0 + (k - 1) * RY;        // interior row of this box's first output
         const bool rows_ok = k > 0 && ir0 + RY <= e;   // every row of the box is an output row
+        bool flag = false;
+        if (k == 0) {   // window of the line's first cell (see Line::prime)
+            line.prime(Cons<T>{sb[0], sb[2 * RY * BW], sb[RY * BW], sb[3 * RY * BW]});
+        }
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
             // normal momentum of the y-sweep is rho*v (plane 2)
             const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
-            const Cons<T> N = line.push(U, hl, lam);
+            Cons<T> N;
+            if constexpr (FAST) {
+                // a flag matters unless the push lies past the task's last
+                // output row (no later output depends on it)
+                bool fi = false, fc = false, ff = false;
+                N = line.template step<false>(U, hl, lam, fi, fc, ff);
+                flag |= (fi | fc | ff) & (rows_ok || k == 0 || ir0 + rr < e);
+            } else {
+                N = line.push(U, hl, lam);
+            }
             ob[rr * 32] = N.r;
             ob[(RY + rr) * 32] = N.mt;
             ob[(2 * RY + rr) * 32] = N.mn;
@@ -534,6 +586,13 @@ __device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorM
                 }
             }
         }
+        if constexpr (FAST) {
+            if (__any_sync(0xffffffffu, flag && col_ok)) {
+                aborted = true;
+                kfail = k;
+                break;
+            }
+        }
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) {
@@ -545,11 +604,31 @@ __device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorM
         }
     }
     if (lane == 0) bulk_wait0();
-    if (timed_out) {
+    if (timed_out || aborted) {
+        // drain the boxes still in flight (bounded)
         const int last = min(kfail + STAGES, nst);
-        for (int k = kfail + 1; k < last; ++k) (void)stage_wait<PERSIST>(bar, k % STAGES, k, STAGES, phase);
+        for (int k = kfail + 1; k < last; ++k) (void)stage_wait<true>(bar, k % STAGES, k, STAGES, phase);
     }
     return YOut<T>{smax, !(Ar<T>::fabs_(ssum) < T(INFINITY)), timed_out};
+}
+
+// The full pass, out of line so that its code stays out of the fast loop.
+template <class T, int S, int RY, int BW, int STAGES>
+__device__ __noinline__ YOut<T> y_task_full(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
+                                            int task, T* buf, T* obuf, uint64_t* bar, uint32_t* phase, int lane) {
+    bool unused = false;
+    return y_pass<T, S, RY, BW, STAGES, false>(tm, tm_out, a, task, buf, obuf, bar, *phase, lane, unused);
+}
+
+// One y-sweep task: the fast pass, and the full pass when the fast one gave
+// up.  Barrier phases are carried in `phase` across both passes.
+template <class T, int S, int RY, int BW, int STAGES>
+__device__ __forceinline__ YOut<T> y_task(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
+                                          int task, T* buf, T* obuf, uint64_t* bar, uint32_t& phase, int lane) {
+    bool aborted = false;
+    YOut<T> o = y_pass<T, S, RY, BW, STAGES, true>(tm, tm_out, a, task, buf, obuf, bar, phase, lane, aborted);
+    if (aborted && !o.timed_out) o = y_task_full<T, S, RY, BW, STAGES>(tm, tm_out, a, task, buf, obuf, bar, &phase, lane);
+    return o;
 }
 
 // y-sweep: Utmp -> Unew (S buffer), one task per warp, with the fused CFL
@@ -580,7 +659,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     }
     __syncwarp();
     uint32_t phase = 0;
-    const YOut<T> o = y_task<T, S, RY, BW, STAGES, false>(&tm, &tm_out, a, task, buf, obuf, bar, phase, lane);
+    const YOut<T> o = y_task<T, S, RY, BW, STAGES>(&tm, &tm_out, a, task, buf, obuf, bar, phase, lane);
     warp_arrive<T>(ctl, o.smax, o.bad, o.timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);
 }
 
@@ -668,7 +747,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) ensemble_kernel(const __grid_co
             const SweepArgs<T>& a = I.ya[1 - cur];
             YOut<T> o{T(0), false, true};
             if (ok)
-                o = y_task<T, S, RY, BWY, SY, true>(&I.tm_y, &I.tm_yo[1 - cur], a, ty - e.y_off[q],
+                o = y_task<T, S, RY, BWY, SY>(&I.tm_y, &I.tm_yo[1 - cur], a, ty - e.y_off[q],
                                                      reinterpret_cast<T*>(wb),
                                                      reinterpret_cast<T*>(wb + SY * YSTAGE), bar, phase, lane);
             warp_arrive<T>(ctl, o.smax, o.bad, o.timed_out, lane, (unsigned)a.ntasks, a.finalize, a.out_index);

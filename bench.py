@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the planner's launch shape (profiling)")
     return ap.parse_args()
 
 
@@ -386,7 +387,7 @@ def run_ours(args, dist: Dist):
 
     # ---- FP32 device-resident throughput (the headline) -------------------
     s32 = E.Solver.for_problem(prob, "fp32", args.solver)
-    shape32 = s32.autotune(10)
+    shape32 = ((s32.get_option("seg_x"), s32.get_option("seg_y")) if args.no_autotune else s32.autotune(10))
     s32.time_steps(W)
     dist.barrier()
     with ClockSampler(dist.local) as clk:
@@ -487,7 +488,7 @@ def run_ours(args, dist: Dist):
                        "cancellation, FP64 exact-solver Newton)", "graph": f"{K} steps in one CUDA graph",
                        "l2": "inputs larger than L2 (1.07 GB per FP32 state buffer vs 126 MB L2)",
                        "parallelism": f"replicas x{dist.ws}",
-                       "seg_xy": list(shape32) + ["autotuned"]},
+                       "seg_xy": list(shape32) + ["planner" if args.no_autotune else "autotuned"]},
             "gpu_launches": 2 * K,
             "adjoint_forward_ratio": (out["adjoint"]["fp32"]["backward_over_forward"]
                                       if "adjoint" in out else None),

@@ -28,9 +28,9 @@ namespace {
 #if EU_PREC == 32
 using T = float;
 #ifndef EU_MINB_X
-#define EU_MINB_X 4
+#define EU_MINB_X 3
 #endif
-constexpr int MINB_X = EU_MINB_X, MINB_Y = 4;   // x: EU_MINB_X CTAs of 4 warps per SM; y: 16 warps (<= 128 registers)
+constexpr int MINB_X = EU_MINB_X, MINB_Y = 4;   // x: 3 CTAs of 4 warps per SM (<= 168 registers, measured 13% faster than 4); y: 16 warps (<= 128 registers)
 #else
 using T = double;
 constexpr int MINB_X = 2, MINB_Y = 2;

@@ -100,6 +100,41 @@ class Dist:
             self.td.destroy_process_group()
 
 
+def bind_to_gpu_cpus(local: int):
+    """Pin this process to the CPUs nvidia-smi reports as local to the GPU,
+    so that pinned host buffers allocated afterwards come from that node's
+    memory (the e2e copies cross the CPU-GPU link, not a socket link).
+    Returns the CPU list used, or None."""
+    try:
+        out = subprocess.run(["nvidia-smi", "topo", "-m"], capture_output=True, text=True, timeout=20).stdout
+    except Exception:
+        return None
+    lines = [l for l in out.splitlines() if l.strip()]
+    if not lines:
+        return None
+    head = lines[0].split("\t")
+    col = next((k for k, h in enumerate(head) if "CPU Affinity" in h), None)
+    row = next((l.split("\t") for l in lines if l.startswith(f"GPU{local}\t") or l.startswith(f"GPU{local} ")), None)
+    if col is None or row is None or col >= len(row):
+        return None
+    cpus = set()
+    for part in row[col].replace(" ", "").split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            if a.isdigit() and b.isdigit():
+                cpus.update(range(int(a), int(b) + 1))
+        elif part.isdigit():
+            cpus.add(int(part))
+    cpus &= set(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else cpus
+    if not cpus:
+        return None
+    try:
+        os.sched_setaffinity(0, cpus)
+    except OSError:
+        return None
+    return row[col].strip()
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
 
@@ -439,6 +474,7 @@ def run_ours(args, dist: Dist):
 
     # ---- e2e through the drop-in call on host grids -----------------------
     if not args.skip_e2e:
+        cpus = bind_to_gpu_cpus(dist.local)
         se = E.Solver.for_problem(prob, "fp32", args.solver)
         A = E.PinnedGrid(n, n)
         B = E.PinnedGrid(n, n)
@@ -454,7 +490,8 @@ def run_ours(args, dist: Dist):
         aos = (n + 4) * (n + 4) * 32
         out["e2e"] = {"value": cells * ke * dist.ws / el, "unit": UNIT, "h2d_bytes_per_step": aos,
                       "d2h_bytes_per_step": aos, "steps": ke,
-                      "call": "eu_step_host (Grid2D AoS in, BC + compute_dt + advance_second_order, AoS out)"}
+                      "call": "eu_step_host (Grid2D AoS in, BC + compute_dt + advance_second_order, AoS out)",
+                      "host_cpus": cpus}
         se.close()
         del A, B
 

@@ -462,6 +462,13 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 // columns, are stored directly.
 // src/cpu/solver_cpu.cpp:247-279 + :474-498
 // ---------------------------------------------------------------------------
+// max(a, b) that returns NaN when either is NaN (PTX max.NaN).
+__device__ __forceinline__ float max_nan(float a, float b) {
+    float d;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+
 // Result of one y-sweep task for the step's epilogue.
 template <class T> struct YOut {
     T smax;
@@ -538,6 +545,7 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
         __syncwarp();
         const int ir0 = r0 + (k - 1) * RY;        // interior row of this box's first output
         const bool rows_ok = k > 0 && ir0 + RY <= e;   // every row of the box is an output row
+        const int nlive = k == 0 ? RY : e - ir0;       // pushes whose flags can reach an output
         bool flag = false;
         if (k == 0) {   // window of the line's first cell (see Line::prime)
             line.prime(Cons<T>{sb[0], sb[2 * RY * BW], sb[RY * BW], sb[3 * RY * BW]});
@@ -552,7 +560,7 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
                 // output row (no later output depends on it)
                 bool fi = false, fc = false, ff = false;
                 N = line.template step<false>(U, hl, lam, fi, fc, ff);
-                flag |= (fi | fc | ff) & (rows_ok || k == 0 || ir0 + rr < e);
+                flag |= (fi | fc | ff) & (rr < nlive);
             } else {
                 N = line.push(U, hl, lam);
             }
@@ -564,8 +572,12 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
             const bool out_ok = col_ok && (rows_ok || (k > 0 && ir < e));
             const T sp = signal_speed_fast(N);
             if (out_ok) {
-                ssum += sp;                       // NaN / inf propagate: checked once at the end
-                smax = Ar<T>::fmax_(smax, sp);
+                if constexpr (sizeof(T) == 4) {
+                    smax = max_nan(smax, sp);     // NaN propagates: checked once at the end
+                } else {
+                    ssum += sp;                   // NaN / inf propagate: checked once at the end
+                    smax = Ar<T>::fmax_(smax, sp);
+                }
             }
             if (special) {                        // warp-uniform: few warps store anything directly
                 if (out_ok && direct) store_cell(a.out, ir + 2, sc, N, 2, 1, false);
@@ -609,7 +621,8 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
         const int last = min(kfail + STAGES, nst);
         for (int k = kfail + 1; k < last; ++k) (void)stage_wait<true>(bar, k % STAGES, k, STAGES, phase);
     }
-    return YOut<T>{smax, !(Ar<T>::fabs_(ssum) < T(INFINITY)), timed_out};
+    const bool bad = sizeof(T) == 4 ? !(smax < T(INFINITY)) : !(Ar<T>::fabs_(ssum) < T(INFINITY));
+    return YOut<T>{smax, bad, timed_out};
 }
 
 // The full pass, out of line so that its code stays out of the fast loop.

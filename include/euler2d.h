@@ -221,6 +221,11 @@ int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]);
  * rule dJ/dtheta = <dJ/dU_0, dU_0/dtheta> (large_sys_eq_opt_gb300/adjoint.py). */
 int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k);
 int eu_batch_adjoint_backward(eu_batch* b, const double* const* dJ_dUN, double* const* dJ_dU0);
+/* Test hook of the failure-detection path (no reference counterpart): with
+ * n > 0 every y-sweep task waits for n more x-sweep tasks than exist, its
+ * bounded wait (2 s) expires, and eu_batch_step returns EU_ERR_TIMEOUT with
+ * the device context intact.  0 restores normal operation. */
+int eu_batch_set_wait_extra(eu_batch* b, int n);
 
 /* ---- drop-in calls on host grids (what the reference's callers pass) ------- */
 /* compute_dt(const Grid2D&, double): upload, reduce, read back dt. */
@@ -262,6 +267,15 @@ int eu_autotune(eu_handle* h, int steps, long long chosen[2]);
  * cell (i, j) of a state buffer at column i+6, row j+2; of the x-sweep output
  * at column i+8).  out == NULL only reports the pitch and plane length. */
 int eu_read_planes(eu_handle* h, int which, void* out, size_t bytes, long long* pitch, long long* plane);
+/* Diagnostics counterpart of eu_read_planes: overwrite the raw planes of a
+ * buffer (bytes = 4 planes), e.g. to plant canary values in the unused
+ * columns and padding and check that no kernel reads or writes them. */
+int eu_write_planes(eu_handle* h, int which, const void* in, size_t bytes);
+/* Restart files (no reference counterpart): the state (Grid2D AoS, FP64),
+ * grid geometry, time and step counter; eu_load_state accepts only a file
+ * of the same grid. */
+int eu_save_state(eu_handle* h, const char* path);
+int eu_load_state(eu_handle* h, const char* path);
 /* Device used by handles created afterwards on the calling thread. */
 int eu_set_device(int device);
 /* Name of device 0 and its SM count, for logs. */

@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/euler2d.h"
 #include "adjoint_kernels.h"
 #include "aux_kernels.h"
@@ -25,6 +27,12 @@ using namespace eu;
 namespace {
 
 thread_local std::string g_err;
+
+// NVTX range for the duration of one ABI call (shows in Nsight timelines).
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
 
 long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
@@ -136,6 +144,7 @@ struct eu_batch {
     bool dirty = true;
     cudaGraphExec_t g = nullptr;
     int gsteps = 0;
+    int wait_extra = 0;
     std::string err;
 };
 
@@ -730,6 +739,7 @@ template <class T> int batch_build_t(eu_batch* b) {
     A.y_off[b->n] = ty;
     A.total_x = tx;
     A.total_y = ty;
+    A.wait_extra = b->wait_extra;
     cudaError_t e = cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(EnsInst<T>) * (size_t)b->n,
                                     cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
@@ -998,6 +1008,7 @@ int eu_compute_dt(eu_handle* h, double cfl, double* dt) {
 }
 
 int eu_advance(eu_handle* h, double dt) {
+    Range range_("eu_advance");
     if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
     if (!(dt >= 0.0) || !std::isfinite(dt)) return fail(h, EU_ERR_INVALID, "dt must be finite and >= 0");
     Ctl& c = *h->hctl;
@@ -1051,6 +1062,7 @@ int eu_advance_first_order_host(eu_handle* h, const double* Uold, double* Unew, 
 }
 
 int eu_step_n(eu_handle* h, long long n, const double* dts) {
+    Range range_("eu_step_n");
     if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
     if (n < 0) return fail(h, EU_ERR_INVALID, "n must be >= 0");
     if (n == 0) return EU_OK;
@@ -1095,6 +1107,7 @@ int eu_step_n(eu_handle* h, long long n, const double* dts) {
 }
 
 int eu_run(eu_handle* h, double t_end, int nsnap, eu_snapshot_cb cb, void* user, eu_run_info* info) {
+    Range range_("eu_run");
     if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
     if (nsnap < 0 || nsnap > kMaxSnap) return fail(h, EU_ERR_INVALID, "nsnap must be in [0, 16]");
     if (!(t_end >= 0.0)) return fail(h, EU_ERR_INVALID, "t_end must be >= 0");
@@ -1178,11 +1191,13 @@ int eu_totals(eu_handle* h, double out[4]) {
 // --- drop-in calls on host grids -----------------------------------------------
 // --- discrete adjoint -----------------------------------------------------------
 int eu_adjoint_forward(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
+    Range range_("eu_adjoint_forward");
     if (int rc = adj_fwd_enqueue(h, nsteps, dts, ckpt_k)) return rc;
     return adj_fwd_finish(h);
 }
 
 int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
+    Range range_("eu_adjoint_backward");
     if (int rc = adj_bwd_enqueue(h, dJ_dUN, dJ_dU0)) return rc;
     return adj_bwd_finish(h, dJ_dU0);
 }
@@ -1217,6 +1232,7 @@ int eu_advance_host(eu_handle* h, const double* Uold, double* Utmp, double* Unew
 
 int eu_step_host(eu_handle* h, const double* U, double* Unext, double cfl, double t, double t_end,
                  double* dt_used) {
+    Range range_("eu_step_host");
     if (!h || !U || !Unext) return fail(h, EU_ERR_INVALID, "null argument");
     int rc = upload_to(h, h->cur, U);
     if (rc) return rc;
@@ -1310,6 +1326,7 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
 // one pass over the trials tunes both sweeps.  The state, time and step
 // counter are restored afterwards.
 int eu_autotune(eu_handle* h, int steps, long long chosen[2]) {
+    Range range_("eu_autotune");
     if (!h || steps < 1) return fail(h, EU_ERR_INVALID, "eu_autotune: bad argument");
     const int CX = h->K.box_x, RY = h->K.ry;
     std::vector<int> cx, cy;
@@ -1444,6 +1461,71 @@ int eu_read_planes(eu_handle* h, int which, void* out, size_t bytes, long long* 
     return EU_OK;
 }
 
+int eu_write_planes(eu_handle* h, int which, const void* in, size_t bytes) {
+    if (!h || !in || which < 0 || which > 2) return fail(h, EU_ERR_INVALID, "bad argument");
+    void* dst = which < 2 ? h->S[which] : h->Tm;
+    const long long pl = which < 2 ? h->plane_s : h->plane_t;
+    const size_t need = (size_t)(4 * pl) * h->esz;
+    if (bytes != need) return fail(h, EU_ERR_INVALID, "eu_write_planes: size must equal the plane set");
+    EU_CUDA(h, cudaMemcpyAsync(dst, in, need, cudaMemcpyHostToDevice, h->st));
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    drop_graphs(h);
+    return EU_OK;
+}
+
+// Binary state file: header, then the Grid2D AoS grid (FP64, ghosts incl.).
+struct StateHeader {
+    char magic[8];          // "EU2DSTAT"
+    int version, nx, ny, prec, solver, bc[4];
+    double x_min, x_max, y_min, y_max, t;
+    long long step;
+};
+
+int eu_save_state(eu_handle* h, const char* path) {
+    if (!h || !path) return fail(h, EU_ERR_INVALID, "bad argument");
+    Range range_("eu_save_state");
+    std::vector<double> aos((size_t)4 * (h->cfg.nx + 4) * (h->cfg.ny + 4));
+    if (int rc = eu_download_aos(h, aos.data())) return rc;
+    StateHeader hd{};
+    std::memcpy(hd.magic, "EU2DSTAT", 8);
+    hd.version = 1;
+    hd.nx = h->cfg.nx; hd.ny = h->cfg.ny; hd.prec = h->prec; hd.solver = h->solver;
+    std::memcpy(hd.bc, h->bc, sizeof(hd.bc));
+    hd.x_min = h->cfg.x_min; hd.x_max = h->cfg.x_max; hd.y_min = h->cfg.y_min; hd.y_max = h->cfg.y_max;
+    if (int rc = ctl_pull_sync(h)) return rc;
+    hd.t = h->hctl->t;
+    hd.step = h->hctl->step;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(h, EU_ERR_INVALID, std::string("eu_save_state: cannot open ") + path);
+    const bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 &&
+                    std::fwrite(aos.data(), sizeof(double), aos.size(), f) == aos.size();
+    const bool closed = std::fclose(f) == 0;
+    if (!ok || !closed) return fail(h, EU_ERR_INVALID, std::string("eu_save_state: write failed: ") + path);
+    return EU_OK;
+}
+
+int eu_load_state(eu_handle* h, const char* path) {
+    if (!h || !path) return fail(h, EU_ERR_INVALID, "bad argument");
+    Range range_("eu_load_state");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(h, EU_ERR_INVALID, std::string("eu_load_state: cannot open ") + path);
+    StateHeader hd{};
+    std::vector<double> aos((size_t)4 * (h->cfg.nx + 4) * (h->cfg.ny + 4));
+    bool ok = std::fread(&hd, sizeof(hd), 1, f) == 1 && std::memcmp(hd.magic, "EU2DSTAT", 8) == 0 && hd.version == 1 &&
+              hd.nx == h->cfg.nx && hd.ny == h->cfg.ny && hd.x_min == h->cfg.x_min && hd.x_max == h->cfg.x_max &&
+              hd.y_min == h->cfg.y_min && hd.y_max == h->cfg.y_max;
+    if (ok) ok = std::fread(aos.data(), sizeof(double), aos.size(), f) == aos.size();
+    std::fclose(f);
+    if (!ok) return fail(h, EU_ERR_INVALID, std::string("eu_load_state: not a state file of this grid: ") + path);
+    if (int rc = eu_upload_aos(h, aos.data())) return rc;
+    ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
+    h->hctl->t = hd.t;
+    h->hctl->step = hd.step;
+    if (int rc = ctl_push(h)) return rc;
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
 int eu_set_device(int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
@@ -1533,6 +1615,7 @@ int eu_batch_start(eu_batch* b) {
 }
 
 int eu_batch_step(eu_batch* b, long long nsteps, int* all_done) {
+    Range range_("eu_batch_step");
     if (!b || nsteps < 0) return bfail(b, EU_ERR_INVALID, "bad argument");
     for (eu_handle* h : b->h)
         if (cudaStreamSynchronize(h->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "instance stream failed");
@@ -1676,6 +1759,17 @@ int eu_batch_adjoint_backward(eu_batch* b, const double* const* dJ_dUN, double* 
     for (int i = 0; i < b->n; ++i)
         if (int rc = adj_bwd_finish(b->h[(size_t)i], dJ_dU0[i]))
             return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+    return EU_OK;
+}
+
+// Test hook of the failure-detection path: with n > 0 every y-sweep task
+// waits for n more x-sweep tasks than exist -- a count nothing reaches -- so
+// its bounded wait expires (2 s), the instance's status records the
+// time-out and eu_batch_step returns EU_ERR_TIMEOUT with the context intact.
+int eu_batch_set_wait_extra(eu_batch* b, int n) {
+    if (!b || n < 0) return bfail(b, EU_ERR_INVALID, "bad argument");
+    b->wait_extra = n;
+    b->dirty = true;
     return EU_OK;
 }
 

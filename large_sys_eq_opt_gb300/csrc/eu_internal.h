@@ -108,6 +108,7 @@ template <class T> struct EnsArgs {
     EnsSched* sched;
     int ninst;
     int total_x, total_y;
+    int wait_extra;            // test hook: y tasks wait for this many x tasks more than exist
     int x_off[kMaxInst + 1];   // prefix sums of the instances' x-sweep tasks
     int y_off[kMaxInst + 1];   // ... and y-sweep tasks
 };

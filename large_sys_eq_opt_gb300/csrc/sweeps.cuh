@@ -752,7 +752,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) ensemble_kernel(const __grid_co
             if (__ldcg(&ctl->done)) continue;
             int ok = 1;
             if (lane == 0) {
-                ok = wait_count_bounded(&e.sched->xdone[q], (unsigned)I.xa.ntasks) ? 1 : 0;
+                ok = wait_count_bounded(&e.sched->xdone[q], (unsigned)(I.xa.ntasks + e.wait_extra)) ? 1 : 0;
                 fence_proxy_async_global();
             }
             ok = __shfl_sync(0xffffffffu, ok, 0);

@@ -57,7 +57,8 @@ EXPORTS = (
     "eu_adjoint_forward", "eu_adjoint_backward", "eu_adjoint_timing", "eu_autotune",
     "eu_batch_create", "eu_batch_destroy", "eu_batch_last_error", "eu_batch_handle", "eu_batch_start",
     "eu_batch_step", "eu_batch_run", "eu_batch_time_steps", "eu_batch_autotune",
-    "eu_batch_adjoint_forward", "eu_batch_adjoint_backward",
+    "eu_batch_adjoint_forward", "eu_batch_adjoint_backward", "eu_batch_set_wait_extra", "eu_write_planes",
+    "eu_save_state", "eu_load_state",
 )
 
 _lib = None
@@ -136,6 +137,10 @@ def load(path: str = LIB_PATH):
     L.eu_batch_autotune.argtypes = [B, C.c_int, C.POINTER(C.c_longlong)]
     L.eu_batch_adjoint_forward.argtypes = [B, C.POINTER(C.c_longlong), C.POINTER(_dp), C.c_int]
     L.eu_batch_adjoint_backward.argtypes = [B, C.POINTER(_dp), C.POINTER(_dp)]
+    L.eu_batch_set_wait_extra.argtypes = [B, C.c_int]
+    L.eu_write_planes.argtypes = [H, C.c_int, C.c_void_p, C.c_size_t]
+    L.eu_save_state.argtypes = [H, C.c_char_p]
+    L.eu_load_state.argtypes = [H, C.c_char_p]
     _lib = L
     return L
 
@@ -293,6 +298,11 @@ class Solver:
         self._check(self._L.eu_get_option(self._h, name.encode(), C.byref(v)))
         return v.value
 
+    def _plane_len(self, which: int) -> int:
+        pitch, plane = C.c_longlong(), C.c_longlong()
+        self._check(self._L.eu_read_planes(self._h, int(which), None, 0, C.byref(pitch), C.byref(plane)))
+        return plane.value
+
     def read_planes(self, which: int) -> np.ndarray:
         """Raw device planes (diagnostics): array [4, rows, pitch] of the
         handle's precision; state buffers hold interior (i, j) at [.., j+2, i+6],
@@ -400,6 +410,16 @@ class Solver:
         return dt.value
 
     # -- measurement ---------------------------------------------------------
+    def write_planes(self, which: int, data: np.ndarray):
+        a = np.ascontiguousarray(data)
+        self._check(self._L.eu_write_planes(self._h, int(which), a.ctypes.data_as(C.c_void_p), a.nbytes))
+
+    def save_state(self, path: str):
+        self._check(self._L.eu_save_state(self._h, str(path).encode()))
+
+    def load_state(self, path: str):
+        self._check(self._L.eu_load_state(self._h, str(path).encode()))
+
     def autotune(self, steps: int = 20):
         """Measure and set the fastest segment lengths; returns (seg_x, seg_y)."""
         out = (C.c_longlong * 2)()
@@ -460,6 +480,9 @@ class Batch:
         ms = C.c_float()
         self._check(self._L.eu_batch_time_steps(self._b, int(nsteps), C.byref(ms)))
         return float(ms.value)
+
+    def set_wait_extra(self, n: int):
+        self._check(self._L.eu_batch_set_wait_extra(self._b, int(n)))
 
     def autotune(self, steps: int = 4):
         out = (C.c_longlong * 2)()

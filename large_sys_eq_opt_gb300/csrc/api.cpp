@@ -151,6 +151,10 @@ struct eu_batch {
 namespace {
 
 int fail(eu_handle* h, int code, const std::string& msg) {
+    // A failed runtime call (e.g. an allocation) stays the thread's "last
+    // error" until read; clear it so that the next launch check of any
+    // handle does not report it again.
+    (void)cudaGetLastError();
     if (h) h->err = msg;
     else g_err = msg;
     return code;
@@ -704,6 +708,7 @@ template <class T> Planes<T> planes_of(const eu_handle* h, void* b) {
 // ensemble: descriptors, launches
 // ---------------------------------------------------------------------------
 int bfail(eu_batch* b, int code, const std::string& msg) {
+    (void)cudaGetLastError();
     if (b) b->err = msg;
     else g_err = msg;
     return code;
@@ -876,7 +881,7 @@ int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limite
     for (int b = 0; b < 2; ++b) {
         e = cudaMalloc(&h->S[b], (size_t)(4 * h->plane_s) * h->esz);
         if (e == cudaSuccess) e = cudaMemsetAsync(h->S[b], 0, (size_t)(4 * h->plane_s) * h->esz, h->st);
-        if (e != cudaSuccess) { g_err = std::string("state buffer: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
+        if (e != cudaSuccess) { (void)cudaGetLastError(); g_err = std::string("state buffer: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
     }
     e = cudaMalloc(&h->Tm, (size_t)(4 * h->plane_t) * h->esz);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->Tm, 0, (size_t)(4 * h->plane_t) * h->esz, h->st);
@@ -885,7 +890,7 @@ int eu_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limite
     if (e == cudaSuccess) e = cudaMalloc(&h->d_part, sizeof(double) * 8 * h->part_blocks);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_tot, sizeof(double) * 4);
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_tot, sizeof(double) * 4);
-    if (e != cudaSuccess) { g_err = std::string("allocation: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
+    if (e != cudaSuccess) { (void)cudaGetLastError(); g_err = std::string("allocation: ") + cudaGetErrorString(e); return bail(EU_ERR_NOMEM); }
     ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
     if (ctl_push(h)) { g_err = h->err; return bail(EU_ERR_CUDA); }
     if (encode_all(h)) {

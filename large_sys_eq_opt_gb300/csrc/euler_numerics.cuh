@@ -443,11 +443,6 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
 //   half step        U -/+ (dt/2dx)(F_R - F_L) as one FMA per component
 //   HLLC star state  E* = [(S-u) E + (S*-u)(q S* + p)] / (S - S*), q = rho (S-u)
 // ---------------------------------------------------------------------------
-// All four finite (NaN and inf propagate through the sum; a sum that only
-// overflows needs |values| ~ 1e38 / 1e308 and is treated as non-finite).
-template <class T> __device__ __forceinline__ bool finite4(T a, T b, T c, T d) {
-    return Ar<T>::fabs_((a + b) + (c + d)) < T(INFINITY);
-}
 // Physicality tests of primitives that came out of c2p_fast.  They need no
 // separate test of u_n and u_t: the pressure is E(g-1) - (g-1)/2 (m_n u_n +
 // m_t u_t), so a non-finite momentum or velocity (u = m / rho with rho above
@@ -519,16 +514,20 @@ __device__ __forceinline__ void face_state(const Prim<T>& W, Cons<T>& U, Cons<T>
     F.e = (U.e + W.p) * W.un;
 }
 
-// Reconstruct the centre cell of (Wm, Wc, Wp) and evolve its face states by
-// half a step.  `nice` must say that all three cells pass nice_cell().
+// Reconstruct the centre cell c of (c-1, c, c+1) and evolve its face states
+// by half a step.  The left difference dm = W(c) - W(c-1) is given (a
+// marching line carries it from the previous cell, whose right difference
+// it is) and the right difference dp = W(c+1) - W(c) is returned.  `nice`
+// must say that all three cells pass nice_cell().
 template <class T>
-__device__ __forceinline__ void reconstruct_fast(const Prim<T>& Wm, const Prim<T>& Wc, const Prim<T>& Wp,
-                                                 T hl, bool nice, Face<T>& L, Face<T>& R, bool& slow) {
+__device__ __forceinline__ void reconstruct_fast(const Prim<T>& dm, const Prim<T>& Wc, const Prim<T>& Wp, T hl,
+                                                   bool nice, Face<T>& L, Face<T>& R, bool& slow, Prim<T>& dp) {
+    dp = Prim<T>{Wp.r - Wc.r, Wp.un - Wc.un, Wp.ut - Wc.ut, Wp.p - Wc.p, T(0)};
     Prim<T> s;
-    s.r = minmod(Wc.r - Wm.r, Wp.r - Wc.r);
-    s.un = minmod(Wc.un - Wm.un, Wp.un - Wc.un);
-    s.ut = minmod(Wc.ut - Wm.ut, Wp.ut - Wc.ut);
-    s.p = minmod(Wc.p - Wm.p, Wp.p - Wc.p);
+    s.r = minmod(dm.r, dp.r);
+    s.un = minmod(dm.un, dp.un);
+    s.ut = minmod(dm.ut, dp.ut);
+    s.p = minmod(dm.p, dp.p);
     const Prim<T> WL{Wc.r - T(0.5) * s.r, Wc.un - T(0.5) * s.un, Wc.ut - T(0.5) * s.ut, Wc.p - T(0.5) * s.p, T(0)};
     const Prim<T> WR{Wc.r + T(0.5) * s.r, Wc.un + T(0.5) * s.un, Wc.ut + T(0.5) * s.ut, Wc.p + T(0.5) * s.p, T(0)};
     Cons<T> UL, FL, UR, FR;
@@ -602,8 +601,11 @@ __device__ __forceinline__ Cons<T> hllc_fast(const Cons<T>& UL, const Prim<T>& V
                     Ar<T>::fabs_(Sstar + rho_star + E_star) < T(INFINITY) && rho_star > T(0) &&
                     !(upL && !left) && !(upR && left);
     slow |= !ok;
-    return Cons<T>{U.mn + Se * (rho_star - U.r), (U.mn * un + p) + Se * (rho_star * Sstar - U.mn),
-                   U.mt * un + Se * (rho_star * ut - U.mt), (U.e + p) * un + Se * (E_star - U.e)};
+    // the tangential momentum flux is u_t times the mass flux on either
+    // side of the contact (rho u_n u_t upwind, rho* S* u_t in the star state)
+    const T Fr = U.mn + Se * (rho_star - U.r);
+    return Cons<T>{Fr, (U.mn * un + p) + Se * (rho_star * Sstar - U.mn), ut * Fr,
+                   (U.e + p) * un + Se * (E_star - U.e)};
 }
 
 template <class T>

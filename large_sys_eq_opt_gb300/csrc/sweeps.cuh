@@ -39,7 +39,7 @@ namespace eu {
 // (head/riemann.hpp:650-672) and cell c-2 is updated with its two face
 // fluxes (src/cpu/solver_cpu.cpp:452-453, :489-490).
 template <class T, int S> struct Line {
-    Prim<T> Wm2, Wm1;   // primitives of cells c-2, c-1 (1/rho unused)
+    Prim<T> dm, Wm1;    // W(c-1) - W(c-2), primitives of cell c-1 (1/rho unused)
     Cons<T> Um1;        // conserved state of cell c-1
     Cons<T> A;          // U(c-2) + lam F(c-5/2): the update of cell c-2 less its right flux
     Face<T> Rp;         // evolved right face state of cell c-2
@@ -47,7 +47,7 @@ template <class T, int S> struct Line {
     bool rp_phys;       // Rp is physical (always true when it came from the fast path)
 
     __device__ __forceinline__ void reset() {
-        Wm2 = Prim<T>{}; Wm1 = Prim<T>{}; Um1 = Cons<T>{}; A = Cons<T>{};
+        dm = Prim<T>{}; Wm1 = Prim<T>{}; Um1 = Cons<T>{}; A = Cons<T>{};
         Rp = Face<T>{};
         nice2 = nice1 = false;
         rp_phys = false;
@@ -60,7 +60,7 @@ template <class T, int S> struct Line {
     __device__ __forceinline__ void prime(const Cons<T>& U0) {
         bool isl = false;
         const Prim<T> W = c2p_fast(U0, isl);
-        Wm2 = W; Wm1 = W;
+        dm = Prim<T>{}; Wm1 = W;
         Um1 = U0;
         A = U0;
         Rp.U = U0;
@@ -84,15 +84,19 @@ template <class T, int S> struct Line {
         Prim<T> W = c2p_fast(U, isl);
         const bool nice = nice_cell(W);
         Face<T> L, R;
-        reconstruct_fast(Wm2, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell);
+        Prim<T> dp;
+        reconstruct_fast(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell, dp);
         Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow_face);
         bool r_phys = true;
+        Prim<T> dnext = dp;   // W(c) - W(c-1) for the next cell
         if constexpr (SLOW) {
             slow_cell |= isl;
             if (__builtin_expect(slow_cell | slow_face, 0)) {
+                const Prim<T> Wm2{Wm1.r - dm.r, Wm1.un - dm.un, Wm1.ut - dm.ut, Wm1.p - dm.p, T(0)};
                 const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl, slow_cell, W, L, R);
                 W = o.W; L = o.L; R = o.R; F = o.F;
                 r_phys = o.r_phys;
+                dnext = Prim<T>{W.r - Wm1.r, W.un - Wm1.un, W.ut - Wm1.ut, W.p - Wm1.p, T(0)};
             }
         } else {
             fi |= isl;
@@ -101,7 +105,8 @@ template <class T, int S> struct Line {
         }
         const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
         A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
-        Wm2 = Wm1; Wm1 = W;
+        dm = dnext;
+        Wm1 = W;
         Um1 = U;
         Rp = R;
         nice2 = nice1; nice1 = nice;

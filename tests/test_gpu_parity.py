@@ -124,7 +124,7 @@ def test_reflective_shock_bubble(E, port, solver):
     assert l1(interior(got)[..., 0], interior(U)[..., 0]) <= 1e-10
 
 
-@pytest.mark.parametrize("shape", [(17, 13), (1, 24), (24, 1), (130, 5), (5, 131)])
+@pytest.mark.parametrize("shape", [(17, 13), (1, 24), (24, 1), (130, 5), (5, 131), (1, 1), (2, 2), (3, 1)])
 def test_odd_sizes_multi_step(E, port, shape):
     nx, ny = shape
     g = Grid(nx, ny, 0.0, 1.0, 0.0, 1.0)
@@ -260,3 +260,33 @@ def test_autotune_keeps_state_and_results(E, prec):
         a.step_n(12)
         b.step_n(12)
         assert np.array_equal(a.download(), b.download())
+
+
+def test_run_with_zero_t_end_takes_no_step(E, port):
+    g = Grid(40, 30, 0.0, 2.0, 0.0, 2.0)
+    U = port.init_blast(g)
+    with E.Solver(cfg_of(g), "fp64", "hllc") as s:
+        s.upload(U)
+        before = s.download()
+        info = s.run(0.0)
+        assert info["steps"] == 0 and info["t"] == 0.0
+        assert np.array_equal(s.download(), before)
+
+
+@pytest.mark.parametrize("nsnap", (1, 3, 16))
+def test_snapshot_schedule_counts(E, port, nsnap):
+    """Snapshots at the first step with t >= t_end k / nsnap
+    (scripts/cpu/main_cpu.cpp:244-261) for 1, 3 and the maximum 16."""
+    g = Grid(64, 48, 0.0, 2.0, 0.0, 2.0)
+    U = port.init_blast(g)
+    ref = port.run(U.copy(), g, 0.8, 0.2, "hllc", nsnap=nsnap, want_snapshots=True)
+    got = {}
+    with E.Solver(cfg_of(g, 0.8, 0.2), "fp64", "hllc") as s:
+        s.upload(U)
+        s.run(0.2, nsnap=nsnap, callback=lambda k, step, t, A: got.__setitem__(k, (step, t, A)))
+    assert sorted(got) == list(range(1, nsnap + 1))
+    for k in range(nsnap):
+        step, t, A = got[k + 1]
+        assert step == ref["snap_step"][k]
+        assert abs(t - ref["snap_t"][k]) <= 1e-14
+        assert l1(interior(A)[..., 0], interior(ref["snapshots"][k])[..., 0]) <= 1e-10

@@ -17,6 +17,9 @@ grid, HLLC, minmod; synthetic initial state evaluated on the device.
            measured HBM copy bandwidth.
   cpu_baseline: the CPU oracle (C restatement of the reference solver, FP64,
            OpenMP over all host cores) on a bounded sample of the workload.
+  flops  : secondary figure, the reference algorithm's arithmetic operations
+           per cell-update (op-counting oracle, committed fixture) times
+           the FP32 throughput.
 
 Multi-GPU: the path is run as independent replicas (one grid per rank, no
 collective on the data path); value is the sum over ranks, timing the max.
@@ -196,6 +199,18 @@ def measured_peaks():
         d = json.load(open(p))
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def reference_flops(solver: str):
+    """Arithmetic operations (add, mul, div, sqrt, pow) per cell-update of the
+    reference algorithm for `solver`, counted by the op-counting build of the
+    restatement on the 256^2 blast (tests/golden/opcounts.json, generated by
+    tests/golden/make_opcounts.py); None when the file is absent."""
+    p = os.path.join(ROOT, "tests", "golden", "opcounts.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return float(d["workloads"]["blast_256"][solver]["arith_per_cell_update"])
 
 
 def profiled_traffic(key: str):
@@ -441,6 +456,14 @@ def run_ours(args, dist: Dist):
                        "per_kernel_ms": {"sweep_x": tx / K, "sweep_y": ty / K},
                        "algorithmic_bytes_per_launch": bytes_per_launch}
     out["clocks"] = clk.summary()
+    fl = reference_flops(args.solver)
+    if fl is not None:
+        # secondary figure: the reference algorithm's arithmetic rate at this
+        # throughput (it repeats work the sweeps do once, so this is an
+        # equivalent rate, not the FP32 pipe's)
+        out["flops"] = {"reference_arith_per_cell_update": fl,
+                        "reference_equivalent_tflops": value * fl / 1e12,
+                        "source": "tests/golden/opcounts.json (op-counting oracle, blast 256^2)"}
     s32.close()
 
     # ---- FP64 throughput + FP32-vs-FP64 error at the final step -----------

@@ -50,6 +50,34 @@ def build(reference: bool | None = None) -> None:
                        stderr=subprocess.DEVNULL)
 
 
+OPC_SO = os.path.join(HERE, "_build", "libopcount_euler2d.so")
+
+
+def op_counts(U: np.ndarray, g: "Grid", cfl: float, t_end: float, solver="hllc", max_steps: int = 0) -> dict:
+    """Floating-point operations of the restatement's time loop
+    (scripts/cpu/main_cpu.cpp:217-262: ghost fill, compute_dt,
+    advance_second_order) on U, advanced in place, counted by category
+    (oracle/opcount.cpp).  Returns dict(steps, counts={category: n})."""
+    lib = C.CDLL(OPC_SO)
+    lib.opc_ncat.restype = C.c_int
+    lib.opc_cat_name.restype = C.c_char_p
+    lib.opc_cat_name.argtypes = [C.c_int]
+    lib.opc_run_counted.restype = C.c_longlong
+    lib.opc_run_counted.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.POINTER(C.c_int), C.c_double, C.c_double, C.c_int, C.c_longlong,
+                                    C.POINTER(C.c_ulonglong)]
+    assert U.dtype == np.float64 and U.flags.c_contiguous and U.shape == g.shape
+    n = lib.opc_ncat()
+    counts = (C.c_ulonglong * n)()
+    bc = (C.c_int * 4)(*[BC[b] if isinstance(b, str) else int(b) for b in g.bc])
+    s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+    steps = lib.opc_run_counted(_p(U), g.nx, g.ny, g.x_min, g.x_max, g.y_min, g.y_max, bc, cfl, t_end, s,
+                                int(max_steps), counts)
+    if steps < 0:
+        raise RuntimeError("compute_dt: non-positive maximum wave speed.")
+    return dict(steps=int(steps), counts={lib.opc_cat_name(k).decode(): int(counts[k]) for k in range(n)})
+
+
 def ref_available() -> bool:
     return os.path.exists(REF_SO)
 

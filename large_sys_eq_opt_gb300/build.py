@@ -52,7 +52,8 @@ def units():
             out.append((os.path.join(CSRC, "adjoint_kernels.cu"), f"adj_{prec}_{solver}.o", flags))
     out.append((os.path.join(CSRC, "aux_kernels.cu"), "aux_kernels.o", []))
     out.append((os.path.join(CSRC, "noalloc.cu"), "noalloc.o", []))
-    out.append((os.path.join(CSRC, "api.cpp"), "api.o", ["-x", "cu"]))
+    for unit in ("runtime", "api", "api_adjoint", "api_batch"):
+        out.append((os.path.join(CSRC, unit + ".cpp"), unit + ".o", ["-x", "cu"]))
     return out
 
 

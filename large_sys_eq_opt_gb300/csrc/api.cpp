@@ -6,798 +6,13 @@
 // stream, and lazily built CUDA graphs of whole steps.  The host never
 // touches a state value on the hot path: dt, t_end clipping and the snapshot
 // schedule live in Ctl and are advanced by the y-sweep's last warp.
-#include <cudaTypedefs.h>
-
-#include <algorithm>
-#include <climits>
-#include <cmath>
-#include <cstdio>
-#include <cstring>
-#include <string>
-#include <vector>
-
-#include <nvtx3/nvToolsExt.h>
-
-#include "../../include/euler2d.h"
-#include "adjoint_kernels.h"
-#include "aux_kernels.h"
+//
+// This unit holds the single-grid entry points; runtime.h lists the other
+// units of the runtime.
+#include "runtime.h"
 
 using namespace eu;
-
-namespace {
-
-thread_local std::string g_err;
-
-// NVTX range for the duration of one ABI call (shows in Nsight timelines).
-struct Range {
-    explicit Range(const char* name) { nvtxRangePushA(name); }
-    ~Range() { nvtxRangePop(); }
-};
-
-long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
-
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            return nullptr;
-        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    }();
-    return fn;
-}
-
-SweepKernels kernels_for(int prec, int solver) {
-    if (prec == EU_FP32) {
-        switch (solver) {
-            case EU_HLLC: return sweep_kernels_32_1();
-            case EU_EXACT: return sweep_kernels_32_2();
-            case EU_FORCE: return sweep_kernels_32_3();
-            default: return sweep_kernels_32_0();
-        }
-    }
-    switch (solver) {
-        case EU_HLLC: return sweep_kernels_64_1();
-        case EU_EXACT: return sweep_kernels_64_2();
-        case EU_FORCE: return sweep_kernels_64_3();
-        default: return sweep_kernels_64_0();
-    }
-}
-
-}  // namespace
-
-struct eu_handle {
-    eu_case cfg{};
-    int prec = EU_FP64, solver = EU_HLL;
-    int bc[4] = {0, 0, 0, 0};
-    size_t esz = 8;
-    double dx = 0, dy = 0;
-    int sm_count = 152;
-    cudaStream_t st = nullptr;
-    long long pitch_s = 0, plane_s = 0, pitch_t = 0, plane_t = 0;
-    void* S[2] = {nullptr, nullptr};
-    void* Tm = nullptr;
-    Ctl* ctl = nullptr;   // device
-    Ctl* hctl = nullptr;  // pinned host mirror
-    double* d_aos = nullptr;
-    double* h_aos = nullptr;  // pinned staging for snapshots
-    double* d_part = nullptr;
-    double* d_tot = nullptr;
-    double* h_tot = nullptr;
-    int part_blocks = 1024;
-    void* snap = nullptr;
-    long long snap_plane = 0, snap_stride = 0;
-    int snap_cap = 0;
-    double* d_frozen = nullptr;
-    long long frozen_cap = 0;
-    double* d_dtlog = nullptr;
-    long long dtlog_cap = 0;
-    CUtensorMap tm_x[2];
-    CUtensorMap tm_y;
-    CUtensorMap tm_xo;     // x-sweep output: Utmp boxes, rows [0, ny+2), columns [0, nx+kTOff)
-    CUtensorMap tm_yo[2];  // y-sweep output: S boxes, columns [0, nx+kSOff) (right ghosts clipped)
-    SweepKernels K{};
-    int seg_x = 0, nseg_x = 0, ntasks_x = 0, ctas_x = 0;
-    int seg_y = 0, nseg_y = 0, ntasks_y = 0, ctas_y = 0;
-    int cur = 0;
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    int gsteps = 0;
-    int l2promo_x = 256, l2promo_y = 256;   // TMA L2 promotion (bytes) of the sweep inputs
-    // Discrete adjoint (eu_adjoint_forward / eu_adjoint_backward): checkpoints
-    // every k steps plus one segment of recomputed forward states.
-    struct Adj {
-        int k = 0, nseg = 0;
-        long long nsteps = 0;
-        std::vector<void*> ck;   // nseg+1 states: ck[s] = state after s*k steps
-        std::vector<void*> R;    // k states: R[j] = state after s*k+j steps (j >= 1) of the ring segment
-        std::vector<void*> Q;    // k x-sweep outputs of the ring segment
-        std::vector<CUtensorMap> ck_x, ck_yo, R_x, R_yo, Q_xo, Q_y;
-        void* lam = nullptr;     // adjoint of the state
-        void* mu = nullptr;      // adjoint of the x-sweep output
-        double* d_dts = nullptr;
-        long long dts_cap = 0;
-        std::vector<double> dts;
-        Ctl* hctl = nullptr;     // pinned control images, one per segment launch
-        int hctl_cap = 0;
-        int ring_seg = -1;
-        bool ready = false;
-        double t0 = 0.0;
-        long long step0 = 0;
-        cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-        float ms_fwd = 0.f, ms_bwd = 0.f;
-    } adj;
-    std::string err;
-};
-
-// Ensemble of independent grids advanced by one persistent launch per step.
-struct eu_batch {
-    int n = 0, prec = EU_FP32, solver = EU_HLLC;
-    std::vector<eu_handle*> h;   // one handle per instance (state, maps, control block)
-    cudaStream_t st = nullptr;
-    SweepKernels K{};
-    void* d_inst = nullptr;      // EnsInst<T>[n]
-    EnsSched* d_sched = nullptr;
-    std::vector<unsigned char> args;   // host image of EnsArgs<T>
-    int ctas = 0;
-    bool dirty = true;
-    cudaGraphExec_t g = nullptr;
-    int gsteps = 0;
-    int wait_extra = 0;
-    std::string err;
-};
-
-namespace {
-
-int fail(eu_handle* h, int code, const std::string& msg) {
-    // A failed runtime call (e.g. an allocation) stays the thread's "last
-    // error" until read; clear it so that the next launch check of any
-    // handle does not report it again.
-    (void)cudaGetLastError();
-    if (h) h->err = msg;
-    else g_err = msg;
-    return code;
-}
-
-int cuda_fail(eu_handle* h, cudaError_t e, const char* what) {
-    return fail(h, e == cudaErrorMemoryAllocation ? EU_ERR_NOMEM : EU_ERR_CUDA,
-                std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define EU_CUDA(h, call)                                        \
-    do {                                                        \
-        cudaError_t e_ = (call);                                \
-        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
-    } while (0)
-
-template <class T> Planes<T> planes_s(const eu_handle* h, int b) {
-    return Planes<T>{static_cast<T*>(h->S[b]), h->pitch_s, h->plane_s};
-}
-template <class T> Planes<T> planes_t(const eu_handle* h) {
-    return Planes<T>{static_cast<T*>(h->Tm), h->pitch_t, h->plane_t};
-}
-
-CUtensorMapL2promotion promo_of(int bytes) {
-    switch (bytes) {
-        case 0: return CU_TENSOR_MAP_L2_PROMOTION_NONE;
-        case 64: return CU_TENSOR_MAP_L2_PROMOTION_L2_64B;
-        case 128: return CU_TENSOR_MAP_L2_PROMOTION_L2_128B;
-        default: return CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
-    }
-}
-
-int encode(eu_handle* h, CUtensorMap* m, void* base, long long width, long long pitch, long long plane,
-           int box_w, int box_h, CUtensorMapSwizzle swz, int promo, long long height = -1) {
-    auto fn = encode_fn();
-    if (!fn) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
-    const cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)(height > 0 ? height : h->cfg.ny + 4), 4};
-    const cuuint64_t strides[2] = {(cuuint64_t)(pitch * h->esz), (cuuint64_t)(plane * h->esz)};
-    const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 4};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r = fn(m, h->prec == EU_FP32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
-                          3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          swz, promo_of(promo),
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(h, EU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-    return EU_OK;
-}
-
-// Width of the y-sweep store map: the interior's end (column nx+kSOff)
-// rounded down to 16 bytes, because TMA stores clip at that granularity and
-// must not reach the right ghost columns.
-long long wclip_of(const eu_handle* h) {
-    const long long per16 = 16 / (long long)h->esz;
-    return std::max<long long>((h->cfg.nx + kSOff) / per16 * per16, per16);
-}
-
-int encode_all(eu_handle* h) {
-    for (int b = 0; b < 2; ++b)
-        if (int rc = encode(h, &h->tm_x[b], h->S[b], h->cfg.nx + kSOff + 2, h->pitch_s, h->plane_s, h->K.box_x, 32,
-                            CU_TENSOR_MAP_SWIZZLE_32B, h->l2promo_x))
-            return rc;
-    // x-sweep stores: width nx+4 and height ny+2 clip everything past the
-    // last interior column / row, so no box spills into the top ghost rows.
-    if (int rc = encode(h, &h->tm_xo, h->Tm, h->cfg.nx + kTOff, h->pitch_t, h->plane_t, h->K.box_x, 32,
-                        CU_TENSOR_MAP_SWIZZLE_32B, 256, h->cfg.ny + 2))
-        return rc;
-    for (int b = 0; b < 2; ++b)
-        if (int rc = encode(h, &h->tm_yo[b], h->S[b], wclip_of(h), h->pitch_s, h->plane_s, 32, h->K.ry,
-                            CU_TENSOR_MAP_SWIZZLE_NONE, 256))
-            return rc;
-    return encode(h, &h->tm_y, h->Tm, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry,
-                  CU_TENSOR_MAP_SWIZZLE_NONE, h->l2promo_y);
-}
-
-// Work decomposition.  Every warp is one task: a segment of one group of 32
-// lines.  Measured on GB300 (8192^2 and 2048^2, FP32 HLLC), launches of many
-// short tasks beat near-single-wave launches of long ones even though each
-// task recomputes a 4-cell warm-up (plus one box in the x-sweep): CTAs refill
-// the SMs as they retire, the tail shrinks to one short task, and fewer
-// lines are in flight at once.  The default aims at about eight tasks per
-// resident warp slot with segments clamped to [32, 128] rows (y) and
-// [32, 256] columns (x); eu_set_option overrides it.
-void plan(eu_handle* h) {
-    const int nx = h->cfg.nx, ny = h->cfg.ny;
-    const long long slots_x = (long long)h->sm_count * h->K.nw * h->K.occ_x();
-    const long long slots_y = (long long)h->sm_count * h->K.nw * h->K.occ_y();
-    const int CX = h->K.box_x;
-    const int rgroups = (ny + 31) / 32;
-    long long want = ((long long)rgroups * nx + 8 * slots_x - 1) / (8 * slots_x);
-    want = std::min<long long>(std::max<long long>(want, 32), 256);
-    int seg = (int)round_up(std::min<long long>(want, nx), CX);
-    h->seg_x = seg;
-    h->nseg_x = (nx + seg - 1) / seg;
-    h->ntasks_x = rgroups * h->nseg_x;
-    h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
-    const int groups = (nx + kSOff + 31) / 32;
-    want = ((long long)groups * ny + 8 * slots_y - 1) / (8 * slots_y);
-    want = std::min<long long>(std::max<long long>(want, 32), 128);
-    h->seg_y = (int)round_up(std::min<long long>(want, ny), h->K.ry);  // whole output boxes
-    h->nseg_y = groups;  // tasks per row segment
-    h->ntasks_y = groups * ((ny + h->seg_y - 1) / h->seg_y);
-    h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
-}
-
-template <class T> SweepArgs<T> x_args(const eu_handle* h, int cur) {
-    SweepArgs<T> a{};
-    a.out = planes_t<T>(h);
-    a.ctl = h->ctl;
-    a.nx = h->cfg.nx;
-    a.ny = h->cfg.ny;
-    a.seg = h->seg_x;
-    a.nseg = h->nseg_x;
-    a.ntasks = h->ntasks_x;
-    a.bc_lo = h->bc[EU_SIDE_BOTTOM];
-    a.bc_hi = h->bc[EU_SIDE_TOP];
-    a.out_index = cur;
-    a.finalize = 0;
-    a.d = h->dx;
-    a.snap = static_cast<T*>(h->snap);
-    a.snap_plane = h->snap_plane;
-    a.snap_stride = h->snap_stride;
-    return a;
-}
-
-template <class T> SweepArgs<T> y_args(const eu_handle* h, int cur) {
-    SweepArgs<T> a{};
-    a.out = planes_s<T>(h, 1 - cur);
-    a.ctl = h->ctl;
-    a.nx = h->cfg.nx;
-    a.ny = h->cfg.ny;
-    a.seg = h->seg_y;
-    a.nseg = h->nseg_y;
-    a.ntasks = h->ntasks_y;
-    a.bc_lo = h->bc[EU_SIDE_LEFT];
-    a.bc_hi = h->bc[EU_SIDE_RIGHT];
-    a.out_index = 1 - cur;
-    a.finalize = 1;
-    a.wclip = (int)wclip_of(h);
-    a.d = h->dy;
-    return a;
-}
-
-cudaError_t launch_x(eu_handle* h, int cur) {
-    if (h->prec == EU_FP32) {
-        const SweepArgs<float> a = x_args<float>(h, cur);
-        return h->K.x(&h->tm_x[cur], &h->tm_xo, &a, h->ctas_x, h->st);
-    }
-    const SweepArgs<double> a = x_args<double>(h, cur);
-    return h->K.x(&h->tm_x[cur], &h->tm_xo, &a, h->ctas_x, h->st);
-}
-
-cudaError_t launch_y(eu_handle* h, int cur) {
-    if (h->prec == EU_FP32) {
-        const SweepArgs<float> a = y_args<float>(h, cur);
-        return h->K.y(&h->tm_y, &h->tm_yo[1 - cur], &a, h->ctas_y, h->st);
-    }
-    const SweepArgs<double> a = y_args<double>(h, cur);
-    return h->K.y(&h->tm_y, &h->tm_yo[1 - cur], &a, h->ctas_y, h->st);
-}
-
-cudaError_t launch_step(eu_handle* h, int cur) {
-    cudaError_t e = launch_x(h, cur);
-    if (e != cudaSuccess) return e;
-    return launch_y(h, cur);
-}
-
-cudaError_t launch_dt(eu_handle* h, int b) {
-    if (h->prec == EU_FP32) return eu::launch_dt<float>(planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->ctl, h->st);
-    return eu::launch_dt<double>(planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->ctl, h->st);
-}
-
-cudaError_t unpack_state(eu_handle* h, int b, double* d_aos) {
-    if (h->prec == EU_FP32)
-        return launch_unpack_aos<float>(planes_s<float>(h, b), kSOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
-    return launch_unpack_aos<double>(planes_s<double>(h, b), kSOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
-}
-
-cudaError_t unpack_tmp(eu_handle* h, double* d_aos) {
-    if (h->prec == EU_FP32)
-        return launch_unpack_aos<float>(planes_t<float>(h), kTOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
-    return launch_unpack_aos<double>(planes_t<double>(h), kTOff, h->cfg.nx, h->cfg.ny, h->bc, d_aos, h->st);
-}
-
-cudaError_t fill_ghosts(eu_handle* h, int b) {
-    if (h->prec == EU_FP32) return launch_fill_ghosts<float>(planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->bc, h->st);
-    return launch_fill_ghosts<double>(planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->bc, h->st);
-}
-
-cudaError_t pack_state(eu_handle* h, int b, const double* d_aos) {
-    if (h->prec == EU_FP32) return launch_pack_aos<float>(d_aos, planes_s<float>(h, b), h->cfg.nx, h->cfg.ny, h->st);
-    return launch_pack_aos<double>(d_aos, planes_s<double>(h, b), h->cfg.nx, h->cfg.ny, h->st);
-}
-
-long long aos_bytes(const eu_handle* h) { return 32LL * (h->cfg.nx + 4) * (h->cfg.ny + 4); }
-
-// Control block defaults for a fresh sequence of steps.
-void ctl_reset(eu_handle* h, int mode, double t_end, long long max_steps) {
-    Ctl& c = *h->hctl;
-    std::memset(&c, 0, sizeof(Ctl));
-    c.t = 0.0;
-    c.dt = 0.0;
-    c.t_end = t_end;
-    c.cfl_dmin = h->cfg.cfl * std::min(h->dx, h->dy);
-    c.mode = mode;
-    c.max_steps = max_steps;
-    c.cur = h->cur;
-    c.dt_log = h->d_dtlog;
-    c.dt_log_cap = h->dtlog_cap;
-}
-
-int ctl_push(eu_handle* h) {
-    EU_CUDA(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->st));
-    return EU_OK;
-}
-
-int ctl_pull_sync(eu_handle* h) {
-    EU_CUDA(h, cudaMemcpyAsync(h->hctl, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
-    EU_CUDA(h, cudaStreamSynchronize(h->st));
-    h->cur = h->hctl->cur;
-    return EU_OK;
-}
-
-int status_code(eu_handle* h) {
-    const int s = h->hctl->status;
-    if (s & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
-    if (s & kStatusNonPhysical) return fail(h, EU_ERR_NONPHYSICAL, "compute_dt: non-positive maximum wave speed.");
-    return EU_OK;
-}
-
-// Graph of `steps` consecutive steps starting from buffer `cur`.
-int build_graph(eu_handle* h, int cur, int steps, cudaGraphExec_t* out) {
-    cudaGraph_t g = nullptr;
-    EU_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaSuccess;
-    for (int s = 0; s < steps && e == cudaSuccess; ++s) e = launch_step(h, (cur + s) & 1);
-    cudaError_t e2 = cudaStreamEndCapture(h->st, &g);
-    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(h, e, "step capture"); }
-    if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
-    return EU_OK;
-}
-
-int graph_for(eu_handle* h, int cur, cudaGraphExec_t* out) {
-    if (!h->gexec[cur]) {
-        int rc = build_graph(h, cur, h->gsteps, &h->gexec[cur]);
-        if (rc) return rc;
-    }
-    *out = h->gexec[cur];
-    return EU_OK;
-}
-
-void drop_graphs(eu_handle* h) {
-    for (auto& g : h->gexec)
-        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
-}
-
-int ensure_aos(eu_handle* h) {
-    if (!h->d_aos) EU_CUDA(h, cudaMalloc(&h->d_aos, aos_bytes(h)));
-    return EU_OK;
-}
-
-int ensure_snapshots(eu_handle* h, int nsnap) {
-    if (nsnap <= h->snap_cap) return EU_OK;
-    if (h->snap) { cudaFree(h->snap); h->snap = nullptr; h->snap_cap = 0; }
-    h->snap_plane = (long long)h->cfg.nx * h->cfg.ny;
-    h->snap_stride = 4 * h->snap_plane;
-    EU_CUDA(h, cudaMalloc(&h->snap, (size_t)nsnap * h->snap_stride * h->esz));
-    h->snap_cap = nsnap;
-    drop_graphs(h);  // graphs bake the snapshot pointer into the x-sweep args
-    if (!h->h_aos) EU_CUDA(h, cudaMallocHost(&h->h_aos, aos_bytes(h)));
-    return ensure_aos(h);
-}
-
-int upload_to(eu_handle* h, int b, const double* aos) {
-    int rc = ensure_aos(h);
-    if (rc) return rc;
-    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, aos, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
-    EU_CUDA(h, pack_state(h, b, h->d_aos));
-    return EU_OK;
-}
-
-int download_from_state(eu_handle* h, int b, double* aos) {
-    int rc = ensure_aos(h);
-    if (rc) return rc;
-    EU_CUDA(h, unpack_state(h, b, h->d_aos));
-    EU_CUDA(h, cudaMemcpyAsync(aos, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
-    return EU_OK;
-}
-
-// ---------------------------------------------------------------------------
-// discrete adjoint: buffers, forward segments, adjoint sweeps
-// ---------------------------------------------------------------------------
-AdjLaunch adj_launcher(int prec, int solver) {
-    static const AdjLaunch f32[4] = {adjoint_sweep_32_0, adjoint_sweep_32_1, adjoint_sweep_32_2, adjoint_sweep_32_3};
-    static const AdjLaunch f64[4] = {adjoint_sweep_64_0, adjoint_sweep_64_1, adjoint_sweep_64_2, adjoint_sweep_64_3};
-    return prec == EU_FP32 ? f32[solver] : f64[solver];
-}
-
-size_t state_bytes(const eu_handle* h) { return (size_t)(4 * h->plane_s) * h->esz; }
-size_t tmp_bytes(const eu_handle* h) { return (size_t)(4 * h->plane_t) * h->esz; }
-
-// TMA maps of a state buffer (x-sweep input, y-sweep output) and of an
-// x-sweep output buffer (x-sweep output, y-sweep input), as encode_all.
-int enc_state(eu_handle* h, void* b, CUtensorMap* xin, CUtensorMap* yout) {
-    if (int rc = encode(h, xin, b, h->cfg.nx + kSOff + 2, h->pitch_s, h->plane_s, h->K.box_x, 32,
-                        CU_TENSOR_MAP_SWIZZLE_32B, h->l2promo_x))
-        return rc;
-    return encode(h, yout, b, wclip_of(h), h->pitch_s, h->plane_s, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE, 256);
-}
-int enc_tmp(eu_handle* h, void* b, CUtensorMap* xout, CUtensorMap* yin) {
-    if (int rc = encode(h, xout, b, h->cfg.nx + kTOff, h->pitch_t, h->plane_t, h->K.box_x, 32,
-                        CU_TENSOR_MAP_SWIZZLE_32B, 256, h->cfg.ny + 2))
-        return rc;
-    return encode(h, yin, b, h->pitch_t, h->pitch_t, h->plane_t, h->K.box_w_y, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE,
-                  h->l2promo_y);
-}
-
-void adj_free(eu_handle* h) {
-    auto& A = h->adj;
-    for (void* p : A.ck) cudaFree(p);
-    for (void* p : A.R) cudaFree(p);
-    for (void* p : A.Q) cudaFree(p);
-    A.ck.clear(); A.R.clear(); A.Q.clear();
-    A.ck_x.clear(); A.ck_yo.clear(); A.R_x.clear(); A.R_yo.clear(); A.Q_xo.clear(); A.Q_y.clear();
-    cudaFree(A.lam); cudaFree(A.mu); cudaFree(A.d_dts);
-    A.lam = A.mu = nullptr;
-    A.d_dts = nullptr;
-    A.dts_cap = 0;
-    cudaFreeHost(A.hctl);
-    A.hctl = nullptr;
-    A.hctl_cap = 0;
-    for (auto& e : A.ev)
-        if (e) { cudaEventDestroy(e); e = nullptr; }
-    A.k = A.nseg = 0;
-    A.ready = false;
-    A.ring_seg = -1;
-}
-
-int adj_alloc_buf(eu_handle* h, size_t bytes, void** p) {
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, h->st);
-    if (e != cudaSuccess) return fail(h, EU_ERR_NOMEM, std::string("adjoint buffers: ") + cudaGetErrorString(e));
-    return EU_OK;
-}
-
-// Buffers for nsteps steps with checkpoints every k steps.
-int adj_prepare(eu_handle* h, long long nsteps, int k) {
-    auto& A = h->adj;
-    const int nseg = (int)((nsteps + k - 1) / k);
-    if (A.k != k || A.nseg < nseg) {
-        EU_CUDA(h, cudaStreamSynchronize(h->st));
-        adj_free(h);
-        A.ck.assign(nseg + 1, nullptr);
-        A.R.assign(k, nullptr);
-        A.Q.assign(k, nullptr);
-        A.ck_x.resize(nseg + 1); A.ck_yo.resize(nseg + 1);
-        A.R_x.resize(k); A.R_yo.resize(k);
-        A.Q_xo.resize(k); A.Q_y.resize(k);
-        for (int i = 0; i <= nseg; ++i) {
-            if (int rc = adj_alloc_buf(h, state_bytes(h), &A.ck[i])) return rc;
-            if (int rc = enc_state(h, A.ck[i], &A.ck_x[i], &A.ck_yo[i])) return rc;
-        }
-        for (int j = 1; j < k; ++j) {
-            if (int rc = adj_alloc_buf(h, state_bytes(h), &A.R[j])) return rc;
-            if (int rc = enc_state(h, A.R[j], &A.R_x[j], &A.R_yo[j])) return rc;
-        }
-        for (int j = 0; j < k; ++j) {
-            if (int rc = adj_alloc_buf(h, tmp_bytes(h), &A.Q[j])) return rc;
-            if (int rc = enc_tmp(h, A.Q[j], &A.Q_xo[j], &A.Q_y[j])) return rc;
-        }
-        if (int rc = adj_alloc_buf(h, state_bytes(h), &A.lam)) return rc;
-        if (int rc = adj_alloc_buf(h, state_bytes(h), &A.mu)) return rc;
-        for (auto& e : A.ev) EU_CUDA(h, cudaEventCreate(&e));
-        A.k = k;
-        A.nseg = nseg;
-    }
-    A.nseg = nseg;
-    if (nsteps > A.dts_cap) {
-        cudaFree(A.d_dts);
-        A.d_dts = nullptr;
-        A.dts_cap = 0;
-        EU_CUDA(h, cudaMalloc(&A.d_dts, sizeof(double) * (size_t)nsteps));
-        A.dts_cap = nsteps;
-    }
-    if (A.hctl_cap < nseg + 1) {
-        EU_CUDA(h, cudaStreamSynchronize(h->st));
-        cudaFreeHost(A.hctl);
-        A.hctl = nullptr;
-        A.hctl_cap = 0;
-        EU_CUDA(h, cudaMallocHost(&A.hctl, sizeof(Ctl) * (size_t)(nseg + 1)));
-        A.hctl_cap = nseg + 1;
-    }
-    A.nsteps = nsteps;
-    return EU_OK;
-}
-
-// Forward steps s*k .. s*k+len-1 from ck[s] with the frozen dts: the x-sweep
-// of step j writes Q[j], the y-sweep writes R[j+1] (ck[s+1] for the last).
-template <class T> cudaError_t adj_segment_t(eu_handle* h, int s) {
-    auto& A = h->adj;
-    const long long n0 = (long long)s * A.k;
-    const int len = (int)std::min<long long>(A.k, A.nsteps - n0);
-    Ctl& c = A.hctl[s];
-    std::memset(&c, 0, sizeof(Ctl));
-    c.t_end = INFINITY;
-    c.cfl_dmin = h->cfg.cfl * std::min(h->dx, h->dy);
-    c.mode = kModeFrozen;
-    c.frozen = A.d_dts;
-    c.n_frozen = A.nsteps;
-    c.frozen_base = 0;
-    c.step = n0;
-    c.dt = A.dts[n0];
-    c.max_steps = LLONG_MAX;
-    cudaError_t e = cudaMemcpyAsync(h->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, h->st);
-    for (int j = 0; j < len && e == cudaSuccess; ++j) {
-        SweepArgs<T> ax = x_args<T>(h, 0);
-        ax.out = Planes<T>{static_cast<T*>(A.Q[j]), h->pitch_t, h->plane_t};
-        ax.snap = nullptr;
-        const CUtensorMap* xin = j == 0 ? &A.ck_x[s] : &A.R_x[j];
-        e = h->K.x(xin, &A.Q_xo[j], &ax, h->ctas_x, h->st);
-        if (e != cudaSuccess) break;
-        const bool last = j == len - 1;
-        void* dst = last ? A.ck[s + 1] : A.R[j + 1];
-        SweepArgs<T> ay = y_args<T>(h, 0);
-        ay.out = Planes<T>{static_cast<T*>(dst), h->pitch_s, h->plane_s};
-        ay.out_index = 0;
-        e = h->K.y(&A.Q_y[j], last ? &A.ck_yo[s + 1] : &A.R_yo[j + 1], &ay, h->ctas_y, h->st);
-    }
-    return e;
-}
-cudaError_t adj_segment(eu_handle* h, int s) {
-    return h->prec == EU_FP32 ? adj_segment_t<float>(h, s) : adj_segment_t<double>(h, s);
-}
-
-// Adjoint of step n = s*k + j (the ring holds segment s): y-sweep adjoint
-// lam -> mu on the x-sweep output Q[j], then x-sweep adjoint mu -> lam on the
-// step's input state.
-cudaError_t adj_step(eu_handle* h, int s, int j) {
-    auto& A = h->adj;
-    const long long n = (long long)s * A.k + j;
-    const AdjLaunch L = adj_launcher(h->prec, h->solver);
-    AdjSweepArgs y{};
-    y.P = A.Q[j]; y.p_pitch = h->pitch_t; y.p_plane = h->plane_t; y.p_coff = kTOff;
-    y.A = A.lam; y.a_pitch = h->pitch_s; y.a_plane = h->plane_s; y.a_coff = kSOff;
-    y.G = A.mu; y.g_pitch = h->pitch_s; y.g_plane = h->plane_s; y.g_coff = kSOff;
-    y.nx = h->cfg.nx; y.ny = h->cfg.ny;
-    y.lam_d = A.dts[n] / h->dy;
-    y.bc_lo = h->bc[EU_SIDE_BOTTOM]; y.bc_hi = h->bc[EU_SIDE_TOP];
-    cudaError_t e = L(1, y, h->st);
-    if (e != cudaSuccess) return e;
-    AdjSweepArgs x{};
-    x.P = j == 0 ? A.ck[s] : A.R[j]; x.p_pitch = h->pitch_s; x.p_plane = h->plane_s; x.p_coff = kSOff;
-    x.A = A.mu; x.a_pitch = h->pitch_s; x.a_plane = h->plane_s; x.a_coff = kSOff;
-    x.G = A.lam; x.g_pitch = h->pitch_s; x.g_plane = h->plane_s; x.g_coff = kSOff;
-    x.nx = h->cfg.nx; x.ny = h->cfg.ny;
-    x.lam_d = A.dts[n] / h->dx;
-    x.bc_lo = h->bc[EU_SIDE_LEFT]; x.bc_hi = h->bc[EU_SIDE_RIGHT];
-    return L(0, x, h->st);
-}
-
-// Enqueue the checkpointed forward on the handle's stream (no host wait).
-int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
-    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
-    if (nsteps < 1 || !dts) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: need nsteps >= 1 and a dt list");
-    if (ckpt_k < 1 || ckpt_k > 1024) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: ckpt_k must be in [1, 1024]");
-    if (h->cfg.nx < 2 || h->cfg.ny < 2) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: the adjoint needs nx, ny >= 2");
-    for (long long i = 0; i < nsteps; ++i)
-        if (!(dts[i] > 0.0) || !(dts[i] < INFINITY))
-            return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: every dt must be positive and finite");
-    auto& A = h->adj;
-    A.ready = false;
-    if (int rc = adj_prepare(h, nsteps, ckpt_k)) return rc;
-    A.dts.assign(dts, dts + nsteps);
-    A.t0 = h->hctl->t;
-    A.step0 = h->hctl->step;
-    EU_CUDA(h, cudaMemcpyAsync(A.d_dts, A.dts.data(), sizeof(double) * (size_t)nsteps, cudaMemcpyHostToDevice, h->st));
-    EU_CUDA(h, fill_ghosts(h, h->cur));   // scripts/cpu/main_cpu.cpp:222
-    EU_CUDA(h, cudaMemcpyAsync(A.ck[0], h->S[h->cur], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
-    EU_CUDA(h, cudaEventRecord(A.ev[0], h->st));
-    for (int s = 0; s < A.nseg; ++s) EU_CUDA(h, adj_segment(h, s));
-    EU_CUDA(h, cudaEventRecord(A.ev[1], h->st));
-    A.ring_seg = A.nseg - 1;
-    EU_CUDA(h, cudaMemcpyAsync(h->S[h->cur], A.ck[A.nseg], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
-    EU_CUDA(h, cudaMemcpyAsync(&A.hctl[A.nseg], h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
-    return EU_OK;
-}
-
-// Wait for the forward; status, timing, the handle's time and step.
-int adj_fwd_finish(eu_handle* h) {
-    auto& A = h->adj;
-    EU_CUDA(h, cudaStreamSynchronize(h->st));
-    EU_CUDA(h, cudaEventElapsedTime(&A.ms_fwd, A.ev[0], A.ev[1]));
-    const Ctl probe = A.hctl[A.nseg];
-    double t = A.t0;
-    for (double d : A.dts) t += d;
-    ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
-    h->hctl->t = t;
-    h->hctl->step = A.step0 + A.nsteps;
-    if (int rc = ctl_push(h)) return rc;
-    if (probe.status & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
-    if (probe.status & kStatusNonFinite) return fail(h, EU_ERR_NONPHYSICAL, "non-finite state in the forward steps");
-    A.ready = true;
-    return EU_OK;
-}
-
-int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
-    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
-    if (!dJ_dUN || !dJ_dU0) return fail(h, EU_ERR_INVALID, "eu_adjoint_backward: null argument");
-    auto& A = h->adj;
-    if (!A.ready) return fail(h, EU_ERR_STATE, "eu_adjoint_backward: call eu_adjoint_forward first");
-    if (int rc = ensure_aos(h)) return rc;
-    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, dJ_dUN, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
-    if (h->prec == EU_FP32) EU_CUDA(h, launch_pack_aos<float>(h->d_aos, Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
-    else EU_CUDA(h, launch_pack_aos<double>(h->d_aos, Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
-    EU_CUDA(h, cudaEventRecord(A.ev[2], h->st));
-    for (int s = A.nseg - 1; s >= 0; --s) {
-        if (A.ring_seg != s) {
-            EU_CUDA(h, adj_segment(h, s));
-            A.ring_seg = s;
-        }
-        const int len = (int)std::min<long long>(A.k, A.nsteps - (long long)s * A.k);
-        for (int j = len - 1; j >= 0; --j) EU_CUDA(h, adj_step(h, s, j));
-    }
-    EU_CUDA(h, cudaEventRecord(A.ev[3], h->st));
-    const int bcz[4] = {0, 0, 0, 0};
-    if (h->prec == EU_FP32) EU_CUDA(h, launch_unpack_aos<float>(Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
-    else EU_CUDA(h, launch_unpack_aos<double>(Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
-    EU_CUDA(h, cudaMemcpyAsync(dJ_dU0, h->d_aos, aos_bytes(h), cudaMemcpyDeviceToHost, h->st));
-    return EU_OK;
-}
-
-int adj_bwd_finish(eu_handle* h, double* dJ_dU0) {
-    auto& A = h->adj;
-    EU_CUDA(h, cudaStreamSynchronize(h->st));
-    EU_CUDA(h, cudaEventElapsedTime(&A.ms_bwd, A.ev[2], A.ev[3]));
-    // the gradient is with respect to the interior; ghost entries are zero
-    const int tnx = h->cfg.nx + 4, tny = h->cfg.ny + 4;
-    for (int j = 0; j < tny; ++j)
-        for (int i = 0; i < tnx; ++i)
-            if (i < 2 || i >= tnx - 2 || j < 2 || j >= tny - 2) std::memset(dJ_dU0 + 4 * ((size_t)j * tnx + i), 0, 32);
-    return EU_OK;
-}
-
-template <class T> Planes<T> planes_of(const eu_handle* h, void* b) {
-    return Planes<T>{static_cast<T*>(b), h->pitch_s, h->plane_s};
-}
-
-// ---------------------------------------------------------------------------
-// ensemble: descriptors, launches
-// ---------------------------------------------------------------------------
-int bfail(eu_batch* b, int code, const std::string& msg) {
-    (void)cudaGetLastError();
-    if (b) b->err = msg;
-    else g_err = msg;
-    return code;
-}
-
-template <class T> int batch_build_t(eu_batch* b) {
-    std::vector<EnsInst<T>> inst((size_t)b->n);
-    EnsArgs<T> A;
-    std::memset(&A, 0, sizeof(A));
-    A.inst = static_cast<const EnsInst<T>*>(b->d_inst);
-    A.sched = b->d_sched;
-    A.ninst = b->n;
-    int tx = 0, ty = 0;
-    for (int i = 0; i < b->n; ++i) {
-        eu_handle* h = b->h[(size_t)i];
-        EnsInst<T>& I = inst[(size_t)i];
-        I.tm_x[0] = h->tm_x[0];
-        I.tm_x[1] = h->tm_x[1];
-        I.tm_xo = h->tm_xo;
-        I.tm_y = h->tm_y;
-        I.tm_yo[0] = h->tm_yo[0];
-        I.tm_yo[1] = h->tm_yo[1];
-        I.xa = x_args<T>(h, 0);
-        I.xa.snap = nullptr;
-        I.ya[0] = y_args<T>(h, 1);   // y_args(h, cur) writes buffer 1 - cur
-        I.ya[1] = y_args<T>(h, 0);
-        A.x_off[i] = tx;
-        A.y_off[i] = ty;
-        tx += h->ntasks_x;
-        ty += h->ntasks_y;
-    }
-    A.x_off[b->n] = tx;
-    A.y_off[b->n] = ty;
-    A.total_x = tx;
-    A.total_y = ty;
-    A.wait_extra = b->wait_extra;
-    cudaError_t e = cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(EnsInst<T>) * (size_t)b->n,
-                                    cudaMemcpyHostToDevice, b->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-    if (e != cudaSuccess) return bfail(b, EU_ERR_CUDA, std::string("ensemble descriptors: ") + cudaGetErrorString(e));
-    b->args.assign(reinterpret_cast<unsigned char*>(&A), reinterpret_cast<unsigned char*>(&A) + sizeof(A));
-    if (b->g) { cudaGraphExecDestroy(b->g); b->g = nullptr; }
-    b->dirty = false;
-    return EU_OK;
-}
-int batch_build(eu_batch* b) { return b->prec == EU_FP32 ? batch_build_t<float>(b) : batch_build_t<double>(b); }
-
-cudaError_t batch_launch(eu_batch* b) {
-    cudaError_t e = cudaMemsetAsync(b->d_sched, 0, sizeof(EnsSched), b->st);
-    if (e != cudaSuccess) return e;
-    return b->K.ens(b->args.data(), b->ctas, b->st);
-}
-
-int batch_graph(eu_batch* b, int steps, cudaGraphExec_t* out) {
-    cudaGraph_t gr = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
-    for (int s = 0; s < steps && e == cudaSuccess; ++s) e = batch_launch(b);
-    cudaError_t e2 = cudaStreamEndCapture(b->st, &gr);
-    if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(out, gr, 0);
-    if (gr) cudaGraphDestroy(gr);
-    if (e != cudaSuccess) return bfail(b, EU_ERR_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(e));
-    return EU_OK;
-}
-
-// Pull every instance's control block; report the first bad status.
-int batch_pull(eu_batch* b, int* all_done) {
-    int done = 1;
-    for (int i = 0; i < b->n; ++i) {
-        eu_handle* h = b->h[(size_t)i];
-        if (ctl_pull_sync(h)) return bfail(b, EU_ERR_CUDA, h->err);
-        const int st = h->hctl->status;
-        if (st & kStatusTimeout) return bfail(b, EU_ERR_TIMEOUT, "instance " + std::to_string(i) + ": a bounded device wait expired");
-        if (st & kStatusNonPhysical)
-            return bfail(b, EU_ERR_NONPHYSICAL, "instance " + std::to_string(i) + ": non-positive maximum wave speed");
-        if (st & kStatusNonFinite)
-            return bfail(b, EU_ERR_NONPHYSICAL, "instance " + std::to_string(i) + ": non-finite state");
-        done &= h->hctl->done ? 1 : 0;
-    }
-    if (all_done) *all_done = done;
-    return EU_OK;
-}
-
-}  // namespace
-
-namespace eu {
-// Message for eu_last_error(NULL), for entry points defined in other units.
-void set_global_error(const char* msg) { g_err = msg; }
-}  // namespace eu
+using namespace eu::rt;
 
 // ===========================================================================
 // C ABI
@@ -1194,26 +409,6 @@ int eu_totals(eu_handle* h, double out[4]) {
 }
 
 // --- drop-in calls on host grids -----------------------------------------------
-// --- discrete adjoint -----------------------------------------------------------
-int eu_adjoint_forward(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
-    Range range_("eu_adjoint_forward");
-    if (int rc = adj_fwd_enqueue(h, nsteps, dts, ckpt_k)) return rc;
-    return adj_fwd_finish(h);
-}
-
-int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
-    Range range_("eu_adjoint_backward");
-    if (int rc = adj_bwd_enqueue(h, dJ_dUN, dJ_dU0)) return rc;
-    return adj_bwd_finish(h, dJ_dU0);
-}
-
-int eu_adjoint_timing(eu_handle* h, float ms[2]) {
-    if (!h || !ms) return fail(h, EU_ERR_INVALID, "eu_adjoint_timing: null argument");
-    ms[0] = h->adj.ms_fwd;
-    ms[1] = h->adj.ms_bwd;
-    return EU_OK;
-}
-
 int eu_compute_dt_host(eu_handle* h, const double* U, double cfl, double* dt) {
     if (!h || !U || !dt) return fail(h, EU_ERR_INVALID, "null argument");
     int rc = upload_to(h, h->cur, U);
@@ -1546,236 +741,6 @@ int eu_host_alloc(size_t bytes, void** p) {
 
 void eu_host_free(void* p) {
     if (p) cudaFreeHost(p);
-}
-
-// --- ensemble ------------------------------------------------------------------
-int eu_batch_create(int n, const eu_case* cfgs, const int* bcs, eu_precision prec, eu_solver solver, eu_batch** out) {
-    if (!out || !cfgs || n < 1 || n > kMaxInst)
-        return bfail(nullptr, EU_ERR_INVALID, "eu_batch_create: need 1 <= n <= 256 instances and their cases");
-    *out = nullptr;
-    eu_batch* b = new eu_batch();
-    b->n = n;
-    b->prec = prec;
-    b->solver = solver;
-    auto bail = [&](int rc) {
-        if (b->err.empty()) b->err = g_err;
-        g_err = b->err;
-        eu_batch_destroy(b);
-        return rc;
-    };
-    for (int i = 0; i < n; ++i) {
-        eu_handle* h = nullptr;
-        const int rc = eu_create(&cfgs[i], prec, solver, EU_LIMITER_MINMOD, bcs ? bcs + 4 * i : nullptr, &h);
-        if (rc != EU_OK) {
-            b->err = "instance " + std::to_string(i) + ": " + g_err;
-            return bail(rc);
-        }
-        b->h.push_back(h);
-    }
-    b->K = b->h[0]->K;
-    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
-    const size_t isz = prec == EU_FP32 ? sizeof(EnsInst<float>) : sizeof(EnsInst<double>);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_inst, isz * (size_t)n);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_sched, sizeof(EnsSched));
-    if (e != cudaSuccess) {
-        b->err = std::string("eu_batch_create: ") + cudaGetErrorString(e);
-        return bail(EU_ERR_NOMEM);
-    }
-    b->ctas = b->h[0]->sm_count * b->K.occ_e();
-    b->gsteps = 4;
-    *out = b;
-    return EU_OK;
-}
-
-void eu_batch_destroy(eu_batch* b) {
-    if (!b) return;
-    if (b->st) cudaStreamSynchronize(b->st);
-    if (b->g) cudaGraphExecDestroy(b->g);
-    for (eu_handle* h : b->h) eu_destroy(h);
-    cudaFree(b->d_inst);
-    cudaFree(b->d_sched);
-    if (b->st) cudaStreamDestroy(b->st);
-    delete b;
-}
-
-const char* eu_batch_last_error(const eu_batch* b) { return b ? b->err.c_str() : g_err.c_str(); }
-
-eu_handle* eu_batch_handle(eu_batch* b, int i) {
-    if (!b || i < 0 || i >= b->n) return nullptr;
-    b->dirty = true;   // the caller may change options of the instance
-    return b->h[(size_t)i];
-}
-
-int eu_batch_start(eu_batch* b) {
-    if (!b) return bfail(nullptr, EU_ERR_INVALID, "null batch");
-    for (int i = 0; i < b->n; ++i) {
-        eu_handle* h = b->h[(size_t)i];
-        ctl_reset(h, kModeCfl, h->cfg.t_end, LLONG_MAX);
-        if (ctl_push(h)) return bfail(b, EU_ERR_CUDA, h->err);
-        cudaError_t e = fill_ghosts(h, h->cur);   // scripts/cpu/main_cpu.cpp:222
-        if (e == cudaSuccess) e = launch_dt(h, h->cur);
-        if (e != cudaSuccess) return bfail(b, EU_ERR_CUDA, std::string("eu_batch_start: ") + cudaGetErrorString(e));
-    }
-    return batch_pull(b, nullptr);
-}
-
-int eu_batch_step(eu_batch* b, long long nsteps, int* all_done) {
-    Range range_("eu_batch_step");
-    if (!b || nsteps < 0) return bfail(b, EU_ERR_INVALID, "bad argument");
-    for (eu_handle* h : b->h)
-        if (cudaStreamSynchronize(h->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "instance stream failed");
-    if (b->dirty)
-        if (int rc = batch_build(b)) return rc;
-    if (!b->g)
-        if (int rc = batch_graph(b, b->gsteps, &b->g)) return rc;
-    long long left = nsteps;
-    cudaError_t e = cudaSuccess;
-    while (left >= b->gsteps && e == cudaSuccess) {
-        e = cudaGraphLaunch(b->g, b->st);
-        left -= b->gsteps;
-    }
-    while (left > 0 && e == cudaSuccess) {
-        e = batch_launch(b);
-        --left;
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-    if (e != cudaSuccess) return bfail(b, EU_ERR_CUDA, std::string("eu_batch_step: ") + cudaGetErrorString(e));
-    return batch_pull(b, all_done);
-}
-
-int eu_batch_run(eu_batch* b, long long max_steps, long long* steps_taken) {
-    if (!b || max_steps < 0) return bfail(b, EU_ERR_INVALID, "bad argument");
-    long long done_steps = 0;
-    int all = 0;
-    while (done_steps < max_steps) {
-        const long long k = std::min<long long>(max_steps - done_steps, 64);
-        if (int rc = eu_batch_step(b, k, &all)) return rc;
-        done_steps += k;
-        if (all) break;
-    }
-    if (steps_taken) *steps_taken = done_steps;
-    return EU_OK;
-}
-
-int eu_batch_time_steps(eu_batch* b, int nsteps, float* ms) {
-    if (!b || !ms || nsteps < 1) return bfail(b, EU_ERR_INVALID, "bad argument");
-    for (eu_handle* h : b->h)
-        if (cudaStreamSynchronize(h->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "instance stream failed");
-    if (b->dirty)
-        if (int rc = batch_build(b)) return rc;
-    cudaGraphExec_t g = nullptr;
-    if (int rc = batch_graph(b, nsteps, &g)) return rc;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    cudaError_t e = cudaEventCreate(&e0);
-    if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    if (e == cudaSuccess) e = cudaEventRecord(e0, b->st);
-    if (e == cudaSuccess) e = cudaGraphLaunch(g, b->st);
-    if (e == cudaSuccess) e = cudaEventRecord(e1, b->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    cudaGraphExecDestroy(g);
-    if (e != cudaSuccess) return bfail(b, EU_ERR_CUDA, std::string("eu_batch_time_steps: ") + cudaGetErrorString(e));
-    return batch_pull(b, nullptr);
-}
-
-// Ensemble autotuner: one segment pair for all instances (clipped to each
-// instance's grid), timed on the whole ensemble step; the instances' states
-// and control blocks are restored afterwards.
-int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]) {
-    if (!b || steps < 1) return bfail(b, EU_ERR_INVALID, "bad argument");
-    const int CX = b->K.box_x, RY = b->K.ry;
-    std::vector<void*> saved((size_t)b->n, nullptr);
-    std::vector<Ctl> ctl0((size_t)b->n);
-    std::vector<int> cur0((size_t)b->n);
-    for (int i = 0; i < b->n; ++i) {
-        eu_handle* h = b->h[(size_t)i];
-        if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaMalloc(&saved[(size_t)i], state_bytes(h)) != cudaSuccess ||
-            cudaMemcpy(saved[(size_t)i], h->S[h->cur], state_bytes(h), cudaMemcpyDeviceToDevice) != cudaSuccess) {
-            for (void* p : saved) cudaFree(p);
-            return bfail(b, EU_ERR_NOMEM, "eu_batch_autotune: state backup failed");
-        }
-        ctl0[(size_t)i] = *h->hctl;
-        cur0[(size_t)i] = h->cur;
-    }
-    auto restore = [&]() {
-        for (int i = 0; i < b->n; ++i) {
-            eu_handle* h = b->h[(size_t)i];
-            cudaMemcpy(h->S[cur0[(size_t)i]], saved[(size_t)i], state_bytes(h), cudaMemcpyDeviceToDevice);
-            h->cur = cur0[(size_t)i];
-            *h->hctl = ctl0[(size_t)i];
-            if (ctl_push(h) == EU_OK) cudaStreamSynchronize(h->st);
-        }
-    };
-    const int cx[] = {CX, 2 * CX, 32, 64, 128, 256}, cy[] = {RY, 2 * RY, 16, 32, 64, 128};
-    float best = INFINITY;
-    int bx = cx[2], by = cy[3];
-    int rc = EU_OK;
-    for (int a = 0; a < 6 && rc == EU_OK; ++a)
-        for (int c = 0; c < 6 && rc == EU_OK; ++c) {
-            if (cx[a] % CX || cy[c] % RY) continue;
-            restore();
-            for (eu_handle* h : b->h) {
-                const long long sx = std::min<long long>(cx[a], round_up(h->cfg.nx, CX));
-                const long long sy = std::min<long long>(cy[c], round_up(h->cfg.ny, RY));
-                if ((rc = eu_set_option(h, "seg_x", sx)) || (rc = eu_set_option(h, "seg_y", sy))) break;
-            }
-            b->dirty = true;
-            float ms = 0;
-            if (rc == EU_OK) rc = eu_batch_time_steps(b, 2, &ms);
-            if (rc == EU_OK) rc = eu_batch_time_steps(b, steps, &ms);
-            if (rc == EU_OK && ms < best) { best = ms; bx = cx[a]; by = cy[c]; }
-        }
-    for (int i = 0; i < b->n && rc == EU_OK; ++i) {
-        eu_handle* h = b->h[(size_t)i];
-        const long long sx = std::min<long long>(bx, round_up(h->cfg.nx, CX));
-        const long long sy = std::min<long long>(by, round_up(h->cfg.ny, RY));
-        rc = eu_set_option(h, "seg_x", sx);
-        if (rc == EU_OK) rc = eu_set_option(h, "seg_y", sy);
-    }
-    restore();
-    for (void* p : saved) cudaFree(p);
-    b->dirty = true;
-    if (rc != EU_OK) return rc;
-    if (chosen) { chosen[0] = bx; chosen[1] = by; }
-    return EU_OK;
-}
-
-// Adjoints of every instance, enqueued on the instances' own streams so that
-// they run concurrently, then awaited.
-int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k) {
-    if (!b || !nsteps || !dts) return bfail(b, EU_ERR_INVALID, "bad argument");
-    if (cudaStreamSynchronize(b->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "batch stream failed");
-    for (int i = 0; i < b->n; ++i)
-        if (int rc = adj_fwd_enqueue(b->h[(size_t)i], nsteps[i], dts[i], ckpt_k))
-            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
-    for (int i = 0; i < b->n; ++i)
-        if (int rc = adj_fwd_finish(b->h[(size_t)i]))
-            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
-    return EU_OK;
-}
-
-int eu_batch_adjoint_backward(eu_batch* b, const double* const* dJ_dUN, double* const* dJ_dU0) {
-    if (!b || !dJ_dUN || !dJ_dU0) return bfail(b, EU_ERR_INVALID, "bad argument");
-    for (int i = 0; i < b->n; ++i)
-        if (int rc = adj_bwd_enqueue(b->h[(size_t)i], dJ_dUN[i], dJ_dU0[i]))
-            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
-    for (int i = 0; i < b->n; ++i)
-        if (int rc = adj_bwd_finish(b->h[(size_t)i], dJ_dU0[i]))
-            return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
-    return EU_OK;
-}
-
-// Test hook of the failure-detection path: with n > 0 every y-sweep task
-// waits for n more x-sweep tasks than exist -- a count nothing reaches -- so
-// its bounded wait expires (2 s), the instance's status records the
-// time-out and eu_batch_step returns EU_ERR_TIMEOUT with the context intact.
-int eu_batch_set_wait_extra(eu_batch* b, int n) {
-    if (!b || n < 0) return bfail(b, EU_ERR_INVALID, "bad argument");
-    b->wait_extra = n;
-    b->dirty = true;
-    return EU_OK;
 }
 
 }  // extern "C"

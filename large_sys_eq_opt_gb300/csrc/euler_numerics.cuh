@@ -258,6 +258,34 @@ __device__ __forceinline__ Cons<T> force_flux(const Cons<T>& UL, const Prim<T>& 
 // ---- exact solver (head/riemann.hpp:331-644), Newton always in FP64 ------
 struct PrimD { double r, un, ut, p, a; };
 
+// With gamma = 1.4 every power the exact solver takes of a pressure ratio is
+// a multiple of 1/7: (g-1)/(2g) = 1/7, -(g+1)/(2g) = -6/7, 1/g = 5/7,
+// 2/(g-1) = 5 and 2g/(g-1) = 7.  So one reciprocal seventh root w = r^(-1/7)
+// and integer powers replace every pow(): r^(1/7) = r w^6, r^(-6/7) = w^6,
+// r^(5/7) = (r^(1/7))^5.  (The reference's FP64 exponents differ from these
+// by 1-2 ulp, which moves a power by under 1e-15 relative.)
+static_assert(kGammaD == 1.4, "the seventh-root forms of the exact solver assume gamma = 1.4");
+template <class T> __device__ __forceinline__ T rroot7(T r);
+template <> __device__ __forceinline__ float rroot7<float>(float r) { return powf(r, -1.0f / 7.0f); }
+// FP64: Newton's iteration for w^-7 = r in its division-free form
+// w <- w (8 - r w^7) / 7 (relative error e -> -4 e^2), seeded with the FP32
+// power (e ~ 3e-7): two steps reach full FP64 precision (a few ulp).
+// Outside the FP32 normal range of the seed, pow().
+template <> __device__ __forceinline__ double rroot7<double>(double r) {
+    if (!(r >= 1.0e-30 && r <= 1.0e30)) return pow(r, -1.0 / 7.0);
+    double w = (double)powf((float)r, -1.0f / 7.0f);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const double w2 = w * w, w3 = w2 * w, w7 = w3 * w3 * w;
+        w = w * (8.0 - r * w7) * (1.0 / 7.0);
+    }
+    return w;
+}
+template <class T> __device__ __forceinline__ T pow5(T x) {
+    const T x2 = x * x;
+    return x2 * x2 * x;
+}
+
 // head/riemann.hpp:331-359
 __device__ __forceinline__ void exact_pressure_function(double p, double rK, double pK, double aK,
                                                         double& f, double& fd) {
@@ -269,8 +297,9 @@ __device__ __forceinline__ void exact_pressure_function(double p, double rK, dou
         fd = q * (1.0 - 0.5 * (p - pK) / (p + B));
     } else {
         const double pratio = p / pK;
-        f = 2.0 * aK / (kGammaD - 1.0) * (pow(pratio, (kGammaD - 1.0) / (2.0 * kGammaD)) - 1.0);
-        fd = (1.0 / (rK * aK)) * pow(pratio, -(kGammaD + 1.0) / (2.0 * kGammaD));
+        const double w = rroot7(pratio), w2 = w * w, w6 = w2 * w2 * w2;   // pratio^(-1/7), ^(-6/7)
+        f = 2.0 * aK / (kGammaD - 1.0) * (pratio * w6 - 1.0);
+        fd = (1.0 / (rK * aK)) * w6;
     }
 }
 
@@ -318,20 +347,24 @@ __device__ __forceinline__ void exact_sample(const Prim<T>& V, T a, T p_star, T 
             p = p_star;
         }
     } else {
-        const T a_star = a * Ar<T>::pow_(p_star / V.p, (g - T(1)) / (T(2) * g));
+        const T pr = p_star / V.p;
+        const T w = rroot7(pr), w2 = w * w;
+        const T z = pr * (w2 * w2 * w2);                      // pr^(1/7) = pr^((g-1)/(2g))
+        const T a_star = a * z;
         const T SH = unK - a;
         const T ST = us - a_star;
         if (T(0) <= SH) {
         } else if (T(0) >= ST) {
-            rho = V.r * Ar<T>::pow_(p_star / V.p, T(1) / g);
+            rho = V.r * pow5(z);                              // pr^(5/7) = pr^(1/g)
             un = us;
             p = p_star;
         } else {
             const T af = T(2) / (g + T(1)) * (a + T(0.5) * (g - T(1)) * unK);
             un = T(2) / (g + T(1)) * (a + T(0.5) * (g - T(1)) * unK);
             const T ar = af / a;
-            rho = V.r * Ar<T>::pow_(ar, T(2) / (g - T(1)));
-            p = V.p * Ar<T>::pow_(ar, T(2) * g / (g - T(1)));
+            const T ar5 = pow5(ar);                           // ar^(2/(g-1))
+            rho = V.r * ar5;
+            p = V.p * (ar5 * (ar * ar));                      // ar^(2g/(g-1))
         }
     }
     un = sgn * un;

@@ -272,6 +272,7 @@ template <> __device__ __forceinline__ float rroot7<float>(float r) { return pow
 // power (e ~ 3e-7): two steps reach full FP64 precision (a few ulp).
 // Outside the FP32 normal range of the seed, pow().
 template <> __device__ __forceinline__ double rroot7<double>(double r) {
+    if (r == 1.0) return 1.0;                 // uniform states: p* equals the side's pressure
     if (!(r >= 1.0e-30 && r <= 1.0e30)) return pow(r, -1.0 / 7.0);
     double w = (double)powf((float)r, -1.0f / 7.0f);
 #pragma unroll
@@ -286,15 +287,21 @@ template <class T> __device__ __forceinline__ T pow5(T x) {
     return x2 * x2 * x;
 }
 
-// head/riemann.hpp:331-359
+// head/riemann.hpp:331-359.  The shock branch divides by p + B once; at
+// p = pK the rarefaction branch is f = 0, fd = 1/(rho_K a_K) exactly (the
+// reference's pow(1, e) is 1), taken without the root.
 __device__ __forceinline__ void exact_pressure_function(double p, double rK, double pK, double aK,
                                                         double& f, double& fd) {
     if (p > pK) {
         const double A = 2.0 / ((kGammaD + 1.0) * rK);
         const double B = (kGammaD - 1.0) / (kGammaD + 1.0) * pK;
-        const double q = sqrt(A / (p + B));
+        const double ipb = 1.0 / (p + B);
+        const double q = sqrt(A * ipb);
         f = (p - pK) * q;
-        fd = q * (1.0 - 0.5 * (p - pK) / (p + B));
+        fd = q * (1.0 - 0.5 * (p - pK) * ipb);
+    } else if (p == pK) {
+        f = 0.0;
+        fd = 1.0 / (rK * aK);
     } else {
         const double pratio = p / pK;
         const double w = rroot7(pratio), w2 = w * w, w6 = w2 * w2 * w2;   // pratio^(-1/7), ^(-6/7)
@@ -318,7 +325,8 @@ static __device__ __noinline__ bool exact_star(const PrimD& L, const PrimD& R, d
         const double p_old = p_star;
         p_star = p_old - f / fd;
         if (!(fabs(p_star) < INFINITY) || p_star <= 0.0) p_star = 0.5 * p_old;
-        if (fabs(p_star - p_old) / (0.5 * (p_star + p_old) + 1.0e-14) < 1.0e-8) break;
+        // |dp| / (mean p + 1e-14) < 1e-8, as a product (the mean is positive)
+        if (fabs(p_star - p_old) < 1.0e-8 * (0.5 * (p_star + p_old) + 1.0e-14)) break;
     }
     if (!(fabs(p_star) < INFINITY) || p_star <= 0.0) return false;
     double fL, fR, dL, dR;

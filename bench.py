@@ -17,6 +17,8 @@ grid, HLLC, minmod; synthetic initial state evaluated on the device.
            measured HBM copy bandwidth.
   cpu_baseline: the CPU oracle (C restatement of the reference solver, FP64,
            OpenMP over all host cores) on a bounded sample of the workload.
+  solvers: step times of HLL, HLLC, exact and FORCE on the same grid, FP32
+           and FP64, and the exact solver's FP32-vs-FP64 error after 220 steps.
   flops  : secondary figure, the reference algorithm's arithmetic operations
            per cell-update (op-counting oracle, committed fixture) times
            the FP32 throughput.
@@ -59,6 +61,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--skip-solvers", action="store_true", help="skip the HLL / exact / FORCE step times")
     ap.add_argument("--no-autotune", action="store_true", help="keep the planner's launch shape (profiling)")
     return ap.parse_args()
 
@@ -422,6 +425,56 @@ def ensemble_leg(E, np, steps=20):
             "batched_adjoint": adj}
 
 
+def pressure(A):
+    r, mu, mv, en = (A[2:-2, 2:-2, k] for k in range(4))
+    return 0.3999999999999999 * (en - 0.5 * (mu * mu + mv * mv) / r)
+
+
+def fp64_and_error(E, np, prob, solver, W, K, dist):
+    """FP64 throughput over K graph-replayed steps after W, and the FP32 form
+    against FP64 after W + K steps on the FP64 dt sequence."""
+    cells = prob.cfg.nx * prob.cfg.ny
+    s64 = E.Solver.for_problem(prob, "fp64", solver)
+    s64.set_dt_log(W + K)
+    s64.time_steps(W)
+    tot64, tx64, ty64 = s64.time_steps(K)
+    v64 = cells * K * dist.ws / (dist.max(tot64) / 1e3)
+    dts = s64.dt_log(W + K)
+    ref = s64.download()
+    s64.close()
+    e32 = E.Solver.for_problem(prob, "fp32", solver)
+    e32.step_n(W + K, dts)
+    got = e32.download()
+    e32.close()
+    drho = np.abs(got[2:-2, 2:-2, 0] - ref[2:-2, 2:-2, 0])
+    dp = np.abs(pressure(got) - pressure(ref))
+    fp64 = {"value": v64, "ms_per_step": tot64 / K, "per_kernel_ms": {"sweep_x": tx64 / K, "sweep_y": ty64 / K}}
+    err = {"steps": W + K, "dt": "FP64 dt sequence replayed",
+           "l1_rho": float(drho.mean()), "linf_rho": float(drho.max()),
+           "l1_p": float(dp.mean()), "linf_p": float(dp.max()), "per_field": field_errors(np, got, ref)}
+    return fp64, err
+
+
+def solvers_leg(E, np, prob, dist):
+    """Step time of every Riemann solver on the benchmark grid, FP32 and FP64
+    (graph-replayed steps, CUDA events), and for the exact solver the FP32
+    form against FP64 after 20 + 200 steps on the FP64 dt sequence."""
+    cells = prob.cfg.nx * prob.cfg.ny
+    res = {}
+    for solver in ("hll", "hllc", "exact", "force"):
+        r = {}
+        for prec, w, k in (("fp32", 3, 10), ("fp64", 1, 3)):
+            s = E.Solver.for_problem(prob, prec, solver)
+            s.time_steps(w)
+            tot, tx, ty = s.time_steps(k)
+            s.close()
+            r[prec] = {"ms_per_step": tot / k, "value": cells * k * dist.ws / (dist.max(tot) / 1e3)}
+        res[solver] = r
+    _, err = fp64_and_error(E, np, prob, "exact", 20, 200, dist)
+    res["exact"]["fp32_vs_fp64"] = err
+    return res
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -468,32 +521,12 @@ def run_ours(args, dist: Dist):
 
     # ---- FP64 throughput + FP32-vs-FP64 error at the final step -----------
     if not args.skip_fp64:
-        s64 = E.Solver.for_problem(prob, "fp64", args.solver)
-        s64.set_dt_log(W + K)
-        s64.time_steps(W)
-        tot64, tx64, ty64 = s64.time_steps(K)
-        v64 = cells * K * dist.ws / (dist.max(tot64) / 1e3)
-        dts = s64.dt_log(W + K)
-        ref = s64.download()
-        s64.close()
-        e32 = E.Solver.for_problem(prob, "fp32", args.solver)
-        e32.step_n(W + K, dts)
-        got = e32.download()
-        e32.close()
+        out["fp64"], out["fp32_vs_fp64"] = fp64_and_error(E, np, prob, args.solver, W, K, dist)
+        out["fp32_vs_fp64"]["speedup"] = value / out["fp64"]["value"]
 
-        def pres(A):
-            r, mu, mv, en = (A[2:-2, 2:-2, k] for k in range(4))
-            return 0.3999999999999999 * (en - 0.5 * (mu * mu + mv * mv) / r)
-
-        drho = np.abs(got[2:-2, 2:-2, 0] - ref[2:-2, 2:-2, 0])
-        dp = np.abs(pres(got) - pres(ref))
-        per_field = field_errors(np, got, ref)
-        out["fp64"] = {"value": v64, "ms_per_step": tot64 / K,
-                       "per_kernel_ms": {"sweep_x": tx64 / K, "sweep_y": ty64 / K}}
-        out["fp32_vs_fp64"] = {"speedup": value / v64, "steps": W + K, "dt": "FP64 dt sequence replayed",
-                               "l1_rho": float(drho.mean()), "linf_rho": float(drho.max()),
-                               "l1_p": float(dp.mean()), "linf_p": float(dp.max()), "per_field": per_field}
-        del got, ref, drho, dp
+    # ---- the other Riemann solvers on the same grid ------------------------
+    if not args.skip_solvers:
+        out["solvers"] = solvers_leg(E, np, prob, dist)
 
     # ---- e2e through the drop-in call on host grids -----------------------
     if not args.skip_e2e:

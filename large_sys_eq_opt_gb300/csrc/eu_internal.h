@@ -36,6 +36,8 @@ struct Ctl {
     int nsnap, next_snap;
     unsigned int snap_req;   // bit k: snapshot k is the state at the start of the next step
     unsigned int snap_taken; // bit k: copied into snapshot storage
+    unsigned int ytask_next; // y-sweep work list: next task to hand out (0 between launches)
+    unsigned int ytask_exit; // y-sweep warps that found the list empty (0 between launches)
     int pad;
     double snap_target[kMaxSnap];
     double snap_time[kMaxSnap];

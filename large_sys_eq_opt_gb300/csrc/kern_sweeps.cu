@@ -63,7 +63,16 @@ static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap* tm_out, co
     auto k = sweep_y_kernel<T, SOL, RY, BWY, SY, NW, MINB_Y>;
     static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
     if (attr != cudaSuccess) return attr;
-    k<<<ctas, NW * 32, kSmemY, s>>>(*tm, *tm_out, *static_cast<const SweepArgs<T>*>(args));
+    // persistent: at most one CTA per resident slot (the warps share the work list)
+    static const int slots = [k]() {
+        int dev = 0, sms = 0, occ = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, NW * 32, kSmemY) != cudaSuccess || occ < 1) occ = 1;
+        return sms * occ;
+    }();
+    k<<<ctas < slots ? ctas : slots, NW * 32, kSmemY, s>>>(*tm, *tm_out, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
 }
 

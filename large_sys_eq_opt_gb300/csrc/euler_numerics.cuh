@@ -378,22 +378,55 @@ __device__ __forceinline__ void exact_sample(const Prim<T>& V, T a, T p_star, T 
     un = sgn * un;
 }
 
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+__device__ __forceinline__ bool same_bits(double a, double b) {
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// Identical left and right states -- every face of a uniform region, where
+// both face states equal the cell state.  There exact_star and exact_sample
+// compute, step by step: the PVRS guess p* = p, f(p*) = 0 (the p = p_K
+// branch), so Newton stops at once with u* = u, and the sample returns the
+// state itself (u = -0 comes back as +0).  The caller takes (rho, u, p)
+// directly.  In IEEE arithmetic these are the full route's sampled bits
+// (checked on 10^6 random states in FP64 and FP32).  In the FP32 form the
+// full route's fast division can leave p*/p an ulp away from 1, which the
+// direct route avoids.  The test excludes the cases where the full path
+// takes another route: a PVRS guess below the 1e-12 floor, and f' below
+// 1e-14.
+template <class T> __device__ __forceinline__ bool exact_uniform(const Prim<T>& VL, const Prim<T>& VR, T aL) {
+    if (!(same_bits(VL.r, VR.r) && same_bits(VL.un, VR.un) && same_bits(VL.ut, VR.ut) && same_bits(VL.p, VR.p)))
+        return false;
+    const double r = VL.r, u = VL.un, p = VL.p, a = aL;
+    const double pv = 0.5 * (p + p) - 0.125 * (u - u) * (r + r) * (a + a);   // exact_star's PVRS guess
+    if (!(pv == p) || !(p >= 1.0e-12)) return false;
+    const double d = 1.0 / (r * a);                                        // f' of either side at p* = p
+    return !(fabs(d + d) < 1.0e-14);
+}
+
 // head/riemann.hpp:601-644
 template <class T>
 __device__ __forceinline__ Cons<T> exact_flux(const Cons<T>& UL, const Prim<T>& VL,
                                               const Cons<T>& UR, const Prim<T>& VR) {
     if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(flux(UL, VL), flux(UR, VR));
     const T aL = sound_speed(VL), aR = sound_speed(VR);
-    const PrimD L{(double)VL.r, (double)VL.un, (double)VL.ut, (double)VL.p, (double)aL};
-    const PrimD R{(double)VR.r, (double)VR.un, (double)VR.ut, (double)VR.p, (double)aR};
-    double ps, us;
-    if (!exact_star(L, R, ps, us)) return hll_flux(UL, VL, UR, VR);
-    const T p_star = T(ps), u_star = T(us);
-    const bool left = us >= 0.0;
-    T rho, un, p;
-    if (left) exact_sample(VL, aL, p_star, u_star, T(1), rho, un, p);
-    else exact_sample(VR, aR, p_star, u_star, T(-1), rho, un, p);
-    const T ut = left ? VL.ut : VR.ut;
+    T rho, un, p, ut;
+    if (exact_uniform(VL, VR, aL)) {
+        rho = VL.r;
+        un = VL.un + T(0);   // the sampled u* of u = -0 is +0
+        p = VL.p;
+        ut = VL.ut;
+    } else {
+        const PrimD L{(double)VL.r, (double)VL.un, (double)VL.ut, (double)VL.p, (double)aL};
+        const PrimD R{(double)VR.r, (double)VR.un, (double)VR.ut, (double)VR.p, (double)aR};
+        double ps, us;
+        if (!exact_star(L, R, ps, us)) return hll_flux(UL, VL, UR, VR);
+        const T p_star = T(ps), u_star = T(us);
+        const bool left = us >= 0.0;
+        if (left) exact_sample(VL, aL, p_star, u_star, T(1), rho, un, p);
+        else exact_sample(VR, aR, p_star, u_star, T(-1), rho, un, p);
+        ut = left ? VL.ut : VR.ut;
+    }
     // make_conserved_from_normal_tangential (head/riemann.hpp:40-64)
     Cons<T> Us;
     Us.r = rho;

@@ -251,7 +251,8 @@ void eu_host_free(void* p);
 /* Launch-shape options of a handle (no reference counterpart): "seg_x"
  * (x-sweep segment length, a multiple of the box width), "seg_y" (y-sweep
  * rows per warp), "l2_promotion_x" / "l2_promotion_y" (TMA L2 promotion in
- * bytes: 0, 64, 128, 256), "graph_steps" (steps per replayed graph).
+ * bytes: 0, 64, 128, 256; defaults 128 and 256), "graph_steps" (steps per
+ * replayed graph).
  * Read-only: "tasks_x", "tasks_y".  Used by the tile-shape autotuner. */
 int eu_set_option(eu_handle* h, const char* name, long long value);
 int eu_get_option(eu_handle* h, const char* name, long long* value);

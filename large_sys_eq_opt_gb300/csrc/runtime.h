@@ -73,7 +73,10 @@ struct eu_handle {
     int cur = 0;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 0;
-    int l2promo_x = 256, l2promo_y = 256;   // TMA L2 promotion (bytes) of the sweep inputs
+    // TMA L2 promotion (bytes) of the sweep inputs.  The x-sweep's boxes are
+    // 32-byte row pieces: promoting them to 128 B measured 1.5% faster than
+    // 256 B at 8192^2 (64 B slower); the y-sweep is insensitive.
+    int l2promo_x = 128, l2promo_y = 256;
     // Discrete adjoint (eu_adjoint_forward / eu_adjoint_backward): checkpoints
     // every k steps plus one segment of recomputed forward states.
     struct Adj {

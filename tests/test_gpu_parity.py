@@ -297,3 +297,29 @@ def test_snapshot_schedule_counts(E, port, nsnap):
         assert step == ref["snap_step"][k]
         assert abs(t - ref["snap_t"][k]) <= 1e-14
         assert l1(interior(A)[..., 0], interior(ref["snapshots"][k])[..., 0]) <= 1e-10
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp32", 1e-5)])
+@pytest.mark.parametrize("solver", SOLVERS)
+def test_uniform_flow_stays_uniform(E, port, solver, prec, tol):
+    """A uniform moving state with transmissive boundaries is a steady
+    solution: every face solves the same Riemann problem (for the exact
+    solver the identical-states route), so the flux differences vanish and
+    ten steps change no cell beyond the rounding of the update (carried as
+    U + lam F_left - lam F_right).  The oracle agrees; dt is the CFL step of
+    the uniform state."""
+    g = Grid(64, 48, 0.0, 2.0, 0.0, 1.5)
+    U = g.zeros()
+    r, u, v, p = 1.3, 0.7, -0.4, 2.1
+    U[...] = (r, r * u, r * v, p / 0.3999999999999999 + 0.5 * r * (u * u + v * v))
+    ref = U.copy()
+    out = port.run(ref, g, 0.8, 1.0, solver, max_steps=10)
+    with E.Solver(cfg_of(g, 0.8, 1.0), prec, solver) as s:
+        s.upload(U)
+        s.set_dt_log(10)
+        s.step_n(10)
+        got = s.download()
+        dts = s.dt_log(10)
+    assert np.all(np.abs(interior(got) - interior(U)) <= tol * np.maximum(np.abs(interior(U)), 1.0))
+    assert np.all(np.abs(interior(ref) - interior(U)) <= 1e-13 * np.maximum(np.abs(interior(U)), 1.0))
+    assert np.allclose(dts, out["dts"], rtol=1e-6 if prec == "fp32" else 1e-14, atol=0)

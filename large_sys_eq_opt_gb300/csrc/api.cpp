@@ -523,8 +523,9 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
 // Measured choice of the launch shape: each trial sets one candidate
 // segment length per sweep and times `steps` graph-replayed steps with CUDA
 // events around every kernel; the x- and y-sweep times are kept apart, so
-// one pass over the trials tunes both sweeps.  The state, time and step
-// counter are restored afterwards.
+// one pass over the trials tunes both sweeps.  Every trial starts from the
+// state, time and step counter of the call, and they are restored
+// afterwards.
 int eu_autotune(eu_handle* h, int steps, long long chosen[2]) {
     Range range_("eu_autotune");
     if (!h || steps < 1) return fail(h, EU_ERR_INVALID, "eu_autotune: bad argument");
@@ -549,6 +550,15 @@ int eu_autotune(eu_handle* h, int steps, long long chosen[2]) {
     const size_t trials = std::max(cx.size(), cy.size());
     for (size_t t = 0; t < trials && rc == EU_OK && e == cudaSuccess; ++t) {
         const int sx = cx[std::min(t, cx.size() - 1)], sy = cy[std::min(t, cy.size() - 1)];
+        // every trial starts from the same state (a solution whose cost per
+        // step changes as it evolves would otherwise favour early trials)
+        if (t > 0) {
+            e = cudaMemcpyAsync(h->S[cur0], saved, state_bytes(h), cudaMemcpyDeviceToDevice, h->st);
+            h->cur = cur0;
+            *h->hctl = ctl0;
+            if (e == cudaSuccess && ctl_push(h) != EU_OK) e = cudaErrorUnknown;
+            if (e != cudaSuccess) break;
+        }
         rc = eu_set_option(h, "seg_x", sx);
         if (rc == EU_OK) rc = eu_set_option(h, "seg_y", sy);
         float ms[3], tx = INFINITY, ty = INFINITY;

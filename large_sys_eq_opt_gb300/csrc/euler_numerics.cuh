@@ -336,6 +336,80 @@ static __device__ __noinline__ bool exact_star(const PrimD& L, const PrimD& R, d
     return fabs(u_star) < INFINITY;
 }
 
+// The FP32 form's p* and u*: Newton's iteration of exact_star in FP32 to a
+// relative step of 1e-5, then one FP64 Newton step from that root, with u*
+// from the FP64 pressure functions linearised there.  The FP32 root is good
+// to about 1e-6 relative (the rarefaction branch cancels in FP32), so the
+// FP64 step leaves p* about 1e-12 from the FP64 iteration's own root, and
+// u* as close: well inside the FP32 rounding of both.  Two FP64 pressure
+// function evaluations per face replace about ten.  Any case off this route
+// (a non-positive or non-finite iterate, no convergence within 12 steps, f'
+// below 1e-14, an FP64 step above 1e-4 of p*) runs the FP64 iteration.
+struct StarD { double p, u; bool ok; };
+
+struct SideF {   // one side's constants for the FP32 pressure function
+    float r, p, a, A, B, ip, iz;   // A, B of the shock branch, 1/p, 1/(rho a)
+};
+__device__ __forceinline__ SideF side_f(float r, float p, float a) {
+    const float g = gam<float>();
+    return SideF{r, p, a, (2.0f / (g + 1.0f)) * Ar<float>::rcp(r), ((g - 1.0f) / (g + 1.0f)) * p,
+                 Ar<float>::rcp(p), Ar<float>::rcp(r * a)};
+}
+__device__ __forceinline__ void exact_pressure_function(float p, const SideF& K, float& f, float& fd) {
+    if (p > K.p) {
+        const float ipb = Ar<float>::rcp(p + K.B);
+        const float q = Ar<float>::sqrt_(K.A * ipb);
+        f = (p - K.p) * q;
+        fd = q * (1.0f - 0.5f * (p - K.p) * ipb);
+    } else if (p == K.p) {
+        f = 0.0f;
+        fd = K.iz;
+    } else {
+        const float w = __powf(p * K.ip, -1.0f / 7.0f), w2 = w * w, w6 = w2 * w2 * w2;
+        f = (2.0f / (gam<float>() - 1.0f)) * K.a * ((p * K.ip) * w6 - 1.0f);
+        fd = K.iz * w6;
+    }
+}
+
+// Scalar arguments: a reference to the caller's face states would make the
+// caller keep them in local memory at every face.
+static __device__ __noinline__ StarD exact_star_mixed(float rL, float uL, float pL, float aL, float rR, float uR,
+                                                      float pR, float aR) {
+    const SideF FL = side_f(rL, pL, aL), FR = side_f(rR, pR, aR);
+    const float du = uR - uL;
+    float p = fmaxf(1.0e-12f, 0.5f * (pL + pR) - 0.125f * du * (rL + rR) * (aL + aR));
+    bool conv = false;
+    for (int iter = 0; iter < 12; ++iter) {
+        float fL, fR, dL, dR;
+        exact_pressure_function(p, FL, fL, dL);
+        exact_pressure_function(p, FR, fR, dR);
+        const float pn = p - (fL + fR + du) * Ar<float>::rcp(dL + dR);
+        if (!(pn > 0.0f && pn < INFINITY)) break;
+        conv = fabsf(pn - p) < 1.0e-5f * (0.5f * (pn + p));
+        p = pn;
+        if (conv) break;
+    }
+    StarD st{0.0, 0.0, false};
+    if (conv) {
+        const double p0 = p;
+        double fL, fR, dL, dR;
+        exact_pressure_function(p0, rL, pL, aL, fL, dL);
+        exact_pressure_function(p0, rR, pR, aR, fR, dR);
+        const double fd = dL + dR;
+        const double dp = -(fL + fR + ((double)uR - (double)uL)) / fd;
+        if (!(fabs(fd) < 1.0e-14) && fabs(dp) <= 1.0e-4 * p0) {
+            st.p = p0 + dp;
+            st.u = 0.5 * ((double)uL + (double)uR + (fR + dR * dp) - (fL + dL * dp));
+            st.ok = fabs(st.u) < INFINITY;
+            if (st.ok) return st;
+        }
+    }
+    const PrimD L{(double)rL, (double)uL, 0.0, (double)pL, (double)aL};
+    const PrimD R{(double)rR, (double)uR, 0.0, (double)pR, (double)aR};
+    st.ok = exact_star(L, R, st.p, st.u);
+    return st;
+}
+
 // head/riemann.hpp:445-591 sampled at xi = 0.  sgn = +1 samples the left
 // wave family, -1 the right one (mirror image: un -> -un).
 template <class T>
@@ -429,10 +503,17 @@ __device__ __forceinline__ Cons<T> exact_flux(const Cons<T>& UL, const Prim<T>& 
         p = VL.p;
         ut = VL.ut;
     } else {
-        const PrimD L{(double)VL.r, (double)VL.un, (double)VL.ut, (double)VL.p, (double)aL};
-        const PrimD R{(double)VR.r, (double)VR.un, (double)VR.ut, (double)VR.p, (double)aR};
         double ps, us;
-        if (!exact_star(L, R, ps, us)) return hll_flux(UL, VL, UR, VR);
+        if constexpr (sizeof(T) == 4) {
+            const StarD st = exact_star_mixed(VL.r, VL.un, VL.p, aL, VR.r, VR.un, VR.p, aR);
+            if (!st.ok) return hll_flux(UL, VL, UR, VR);
+            ps = st.p;
+            us = st.u;
+        } else {
+            const PrimD L{(double)VL.r, (double)VL.un, (double)VL.ut, (double)VL.p, (double)aL};
+            const PrimD R{(double)VR.r, (double)VR.un, (double)VR.ut, (double)VR.p, (double)aR};
+            if (!exact_star(L, R, ps, us)) return hll_flux(UL, VL, UR, VR);
+        }
         const T p_star = T(ps), u_star = T(us);
         const bool left = us >= 0.0;
         if (left) exact_sample(VL, aL, p_star, u_star, T(1), rho, un, p);

@@ -106,30 +106,41 @@ int encode_all(eu_handle* h) {
                   CU_TENSOR_MAP_SWIZZLE_NONE, h->l2promo_y);
 }
 
-// Work decomposition.  Every warp is one task: a segment of one group of 32
-// lines.  Measured on GB300 (8192^2 and 2048^2, FP32 HLLC), launches of many
+// Work decomposition.  A task is a segment of one group of 32 lines (the
+// x-sweep runs one per warp, the y-sweep's warps take them from a work
+// list).  Measured on GB300 (8192^2 and 2048^2, FP32 HLLC), launches of many
 // short tasks beat near-single-wave launches of long ones even though each
 // task recomputes a 4-cell warm-up (plus one box in the x-sweep): CTAs refill
 // the SMs as they retire, the tail shrinks to one short task, and fewer
 // lines are in flight at once.  The default aims at about eight tasks per
 // resident warp slot with segments clamped to [32, 128] rows (y) and
-// [32, 256] columns (x); eu_set_option overrides it.
+// [32, 256] columns (x).  The FP32 exact solver is the exception: its faces
+// on and near waves run the Newton iteration for p* (with an FP64 step)
+// while the rest take the identical-states route, so a step lasts about as
+// long as the warps whose lines run along a wave, and short tasks shorten
+// that critical path.  It aims at about 64 tasks per slot with segments
+// down to 8 rows and 16 columns (blast, ms per step: 8192^2 3.2 -> 2.3,
+// 2048^2 0.76 -> 0.64).  The FP64 exact solver is bound by the FP64 pipe
+// throughout and keeps the default.  eu_set_option overrides the plan.
 void plan(eu_handle* h) {
     const int nx = h->cfg.nx, ny = h->cfg.ny;
+    const bool fine = h->solver == EU_EXACT && h->prec == EU_FP32;
+    const long long per_slot = fine ? 64 : 8;
+    const long long min_x = fine ? 16 : 32, min_y = fine ? 8 : 32;
     const long long slots_x = (long long)h->sm_count * h->K.nw * h->K.occ_x();
     const long long slots_y = (long long)h->sm_count * h->K.nw * h->K.occ_y();
     const int CX = h->K.box_x;
     const int rgroups = (ny + 31) / 32;
-    long long want = ((long long)rgroups * nx + 8 * slots_x - 1) / (8 * slots_x);
-    want = std::min<long long>(std::max<long long>(want, 32), 256);
+    long long want = ((long long)rgroups * nx + per_slot * slots_x - 1) / (per_slot * slots_x);
+    want = std::min<long long>(std::max<long long>(want, min_x), 256);
     int seg = (int)round_up(std::min<long long>(want, nx), CX);
     h->seg_x = seg;
     h->nseg_x = (nx + seg - 1) / seg;
     h->ntasks_x = rgroups * h->nseg_x;
     h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
     const int groups = (nx + kSOff + 31) / 32;
-    want = ((long long)groups * ny + 8 * slots_y - 1) / (8 * slots_y);
-    want = std::min<long long>(std::max<long long>(want, 32), 128);
+    want = ((long long)groups * ny + per_slot * slots_y - 1) / (per_slot * slots_y);
+    want = std::min<long long>(std::max<long long>(want, min_y), 128);
     h->seg_y = (int)round_up(std::min<long long>(want, ny), h->K.ry);  // whole output boxes
     h->nseg_y = groups;  // tasks per row segment
     h->ntasks_y = groups * ((ny + h->seg_y - 1) / h->seg_y);

@@ -339,12 +339,12 @@ static __device__ __noinline__ bool exact_star(const PrimD& L, const PrimD& R, d
 // The FP32 form's p* and u*: Newton's iteration of exact_star in FP32 to a
 // relative step of 1e-5, then one FP64 Newton step from that root, with u*
 // from the FP64 pressure functions linearised there.  The FP32 root is good
-// to about 1e-6 relative (the rarefaction branch cancels in FP32), so the
-// FP64 step leaves p* about 1e-12 from the FP64 iteration's own root, and
-// u* as close: well inside the FP32 rounding of both.  Two FP64 pressure
-// function evaluations per face replace about ten.  Any case off this route
-// (a non-positive or non-finite iterate, no convergence within 12 steps, f'
-// below 1e-14, an FP64 step above 1e-4 of p*) runs the FP64 iteration.
+// to about 1e-6 relative (the sum fL + fR + du cancels in FP32), so p* lands
+// about 1e-12 from the FP64 iteration's own root, and u* as close: well
+// inside the FP32 rounding of both.  Two FP64 pressure function evaluations
+// per face replace about ten.  Any case off this route (a non-positive or
+// non-finite iterate, no convergence within 12 steps, f' below 1e-14, an
+// FP64 step above 1e-5 of p*) runs the FP64 iteration.
 struct StarD { double p, u; bool ok; };
 
 struct SideF {   // one side's constants for the FP32 pressure function
@@ -365,9 +365,12 @@ __device__ __forceinline__ void exact_pressure_function(float p, const SideF& K,
         f = 0.0f;
         fd = K.iz;
     } else {
-        const float w = __powf(p * K.ip, -1.0f / 7.0f), w2 = w * w, w6 = w2 * w2 * w2;
-        f = (2.0f / (gam<float>() - 1.0f)) * K.a * ((p * K.ip) * w6 - 1.0f);
-        fd = K.iz * w6;
+        // z - 1 = (p/pK)^(1/7) - 1 from p - pK directly: accurate where p is
+        // near pK and the difference z - 1 would cancel
+        const float d = (p - K.p) * K.ip;                       // p/pK - 1
+        const float zm1 = expm1f(log1pf(d) * (1.0f / 7.0f));
+        f = (2.0f / (gam<float>() - 1.0f)) * K.a * zm1;
+        fd = K.iz * (1.0f + zm1) * Ar<float>::rcp(1.0f + d);   // (p/pK)^(-6/7) / (rho a)
     }
 }
 
@@ -397,7 +400,9 @@ static __device__ __noinline__ StarD exact_star_mixed(float rL, float uL, float 
         exact_pressure_function(p0, rR, pR, aR, fR, dR);
         const double fd = dL + dR;
         const double dp = -(fL + fR + ((double)uR - (double)uL)) / fd;
-        if (!(fabs(fd) < 1.0e-14) && fabs(dp) <= 1.0e-4 * p0) {
+        // |f''| p / (2 f') is below 1 on both branches, so a step of at most
+        // 1e-5 p0 leaves p0 + dp within 1e-10 of the root
+        if (!(fabs(fd) < 1.0e-14) && fabs(dp) <= 1.0e-5 * p0) {
             st.p = p0 + dp;
             st.u = 0.5 * ((double)uL + (double)uR + (fR + dR * dp) - (fL + dL * dp));
             st.ok = fabs(st.u) < INFINITY;

@@ -52,7 +52,25 @@ template <class T> struct C4 { T r, mn, mt, e; };   // conserved, sweep-local
 template <class T> struct W4 { T r, un, ut, p; };   // primitive, sweep-local
 
 template <class T> EUA_HD T sq(T x) { return x * x; }
-template <class T> EUA_HD bool fin(T x) { return fabs(x) < T(INFINITY); }
+// On the device the FP64 tests below run on the integer pipes (bit
+// patterns; the FP64 pipe is this part's narrowest), with the results of the
+// comparisons they replace.
+template <class T> EUA_HD bool fin(T x) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(T) == 8) return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000;
+#endif
+    return fabs(x) < T(INFINITY);
+}
+// floor < x < inf for a finite floor >= 0
+template <class T> EUA_HD bool in_range(T x, T floor) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(T) == 8) {
+        const long long i = __double_as_longlong(x);
+        return i > __double_as_longlong(floor) && i < 0x7ff0000000000000ll;
+    }
+#endif
+    return x > floor && x < T(INFINITY);
+}
 template <class T> EUA_HD T tsqrt(T x) { return sqrt(x); }
 template <class T> EUA_HD T tpow(T a, T b) { return pow(a, b); }
 
@@ -86,12 +104,11 @@ template <class T> EUA_HD C4<T> flux(const C4<T>& U, const W4<T>& W) {
 template <class T> EUA_HD T sound(const W4<T>& W) { return tsqrt(T(kG) * W.p / W.r); }
 // head/riemann.hpp:74-81
 template <class T> EUA_HD bool phys_riemann(const W4<T>& W) {
-    return fin(W.un) && fin(W.ut) && W.r > T(0) && W.p > T(0) && W.r < T(INFINITY) && W.p < T(INFINITY);
+    return fin(W.un) && fin(W.ut) && in_range(W.r, T(0)) && in_range(W.p, T(0));
 }
 // src/cpu/solver_cpu.cpp:39-43
 template <class T> EUA_HD bool phys_recon(const W4<T>& W) {
-    return fin(W.un) && fin(W.ut) && W.r > T(kFloor) && W.p > T(kFloor) && W.r < T(INFINITY) &&
-           W.p < T(INFINITY);
+    return fin(W.un) && fin(W.ut) && in_range(W.r, T(kFloor)) && in_range(W.p, T(kFloor));
 }
 template <class T> EUA_HD C4<T> avg(const C4<T>& a, const C4<T>& b) {
     return C4<T>{T(0.5) * (a.r + b.r), T(0.5) * (a.mn + b.mn), T(0.5) * (a.mt + b.mt), T(0.5) * (a.e + b.e)};
@@ -134,7 +151,21 @@ template <class T> EUA_HD void sound_vjp(const W4<T>& W, T a, T ab, W4<T>& Wb) {
 // reconstruction (src/cpu/solver_cpu.cpp:22-99)
 // ---------------------------------------------------------------------------
 // minmod with the index of the selected argument: 0 none, 1 a, 2 b
+// (On the device in FP64: equal signs, both non-zero and neither NaN, in
+// place of a * b > 0 -- the same except for same-sign pairs whose product
+// underflows, below 1e-308, where it agrees with the forward sweeps.)
 template <class T> EUA_HD T minmod_sel(T a, T b, int& sel) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(T) == 8) {
+        const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+        const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
+        const long long inf = 0x7ff0000000000000ll;
+        if (!((ia ^ ib) >= 0 && ma != 0 && mb != 0 && ma <= inf && mb <= inf)) { sel = 0; return T(0); }
+        if (ma <= mb) { sel = 1; return a; }
+        sel = 2;
+        return b;
+    }
+#endif
     if (!(a * b > T(0))) { sel = 0; return T(0); }
     if (fabs(a) <= fabs(b)) { sel = 1; return a; }
     sel = 2;

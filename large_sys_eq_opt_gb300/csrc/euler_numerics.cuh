@@ -43,13 +43,41 @@ template <class T> struct Prim { T r, un, ut, p, ir; };   // ir = 1/rho when kno
 // ---------------------------------------------------------------------------
 template <class T> struct Ar;
 
+// FP64 comparisons run on the integer pipes, off the FP64 pipe (this part's
+// narrowest): non-negative doubles order like their bit patterns as
+// integers, negative ones in reverse, and the patterns whose magnitude lies
+// above +inf's are the NaNs.  Each helper has the IEEE comparison's result
+// for every input, NaN included; fmin_/fmax_ return the other argument for
+// one NaN, as fmin/fmax do, and differ from them at most in the sign of a
+// zero result.
 template <> struct Ar<double> {
+    static constexpr long long kInf = 0x7ff0000000000000ll;
+    static constexpr long long kMag = 0x7fffffffffffffffll;
+    static __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+    static __device__ __forceinline__ bool nan_(long long i) { return (i & kMag) > kInf; }
+    // total-order key: increasing with the value (-0 below +0)
+    static __device__ __forceinline__ long long key(long long i) { return i ^ ((i >> 63) & kMag); }
     static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
     static __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
-    static __device__ __forceinline__ double fmin_(double a, double b) { return fmin(a, b); }
-    static __device__ __forceinline__ double fmax_(double a, double b) { return fmax(a, b); }
-    static __device__ __forceinline__ bool finite(double x) { return fabs(x) < INFINITY; }
+    static __device__ __forceinline__ double fmin_(double a, double b) {
+        const long long ia = bits(a), ib = bits(b);
+        return (nan_(ib) || (!nan_(ia) && key(ia) <= key(ib))) ? a : b;
+    }
+    static __device__ __forceinline__ double fmax_(double a, double b) {
+        const long long ia = bits(a), ib = bits(b);
+        return (nan_(ib) || (!nan_(ia) && key(ia) >= key(ib))) ? a : b;
+    }
+    // x > c for a finite c >= 0
+    static __device__ __forceinline__ bool gt(double x, double c) {
+        const long long i = bits(x);
+        return i > bits(c) && i <= kInf;
+    }
+
+    // exponent field not all ones (on the integer pipes)
+    static __device__ __forceinline__ bool finite(double x) {
+        return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000;
+    }
     static __device__ __forceinline__ double pow_(double a, double b) { return pow(a, b); }
     static __device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
 };
@@ -158,6 +186,23 @@ template <class T> __device__ __forceinline__ bool physical_riemann(const Prim<T
 template <class T> __device__ __forceinline__ bool physical_recon(const Prim<T>& V) {
     return Ar<T>::finite(V.un) && Ar<T>::finite(V.ut) && V.r > T(kRhoFloorD) &&
            V.p > T(kPFloorD) && V.r < T(INFINITY) && V.p < T(INFINITY);
+}
+
+// FP64: the same tests on the integer pipes (non-negative doubles order like
+// their bit patterns as signed integers; negative ones and -0 have negative
+// patterns; +inf and the NaNs lie at and above 0x7ff0...).
+__device__ __forceinline__ bool finite_above(double x, double floor) {
+    const long long ix = __double_as_longlong(x);
+    return ix > __double_as_longlong(floor) && ix < Ar<double>::kInf;
+}
+template <> __device__ __forceinline__ bool physical_riemann<double>(const Prim<double>& V) {
+    return Ar<double>::finite(V.un) && Ar<double>::finite(V.ut) && finite_above(V.r, 0.0) &&
+           finite_above(V.p, 0.0);
+}
+template <> __device__ __forceinline__ bool physical_recon<double>(const Prim<double>& V) {
+    static_assert(kRhoFloorD == kPFloorD, "one floor for rho and p");
+    return Ar<double>::finite(V.un) && Ar<double>::finite(V.ut) && finite_above(V.r, kRhoFloorD) &&
+           finite_above(V.p, kPFloorD);
 }
 
 // ---------------------------------------------------------------------------
@@ -558,6 +603,17 @@ template <class T> __device__ __forceinline__ T minmod(T a, T b) {
     // same-sign pairs whose product underflows, below 1e-308 in FP64.)
     return Ar<T>::fmax_(T(0), Ar<T>::fmin_(a, b)) + Ar<T>::fmin_(T(0), Ar<T>::fmax_(a, b));
 }
+// FP64: the same selection on the integer pipes, off the narrow FP64 pipe.
+// Equal sign bits and a smaller magnitude (the bit patterns without the
+// sign order like the magnitudes) pick the argument; the value is that of
+// the form above for every non-NaN pair, up to the sign of a zero result.
+template <> __device__ __forceinline__ double minmod<double>(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const unsigned long long ma = (unsigned long long)ia & 0x7fffffffffffffffull;
+    const unsigned long long mb = (unsigned long long)ib & 0x7fffffffffffffffull;
+    const long long r = ma < mb ? ia : ib;
+    return (ia ^ ib) >= 0 ? __longlong_as_double(r) : 0.0;
+}
 
 // Face states of one cell: the half-step-evolved left/right boundary states
 // and their primitives.
@@ -624,6 +680,10 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
 // EU_ERR_NONPHYSICAL through the y-sweep's finiteness check of its outputs.
 template <class T> __device__ __forceinline__ bool phys_above(const Prim<T>& V, T floor) {
     return (V.r > floor) & (V.p > floor);
+}
+// FP64: the same tests on the integer pipes (Ar<double>::gt).
+template <> __device__ __forceinline__ bool phys_above<double>(const Prim<double>& V, double floor) {
+    return Ar<double>::gt(V.r, floor) & Ar<double>::gt(V.p, floor);
 }
 // physical_recon, with the 1e-12 floors (src/cpu/solver_cpu.cpp:39-43)
 template <class T> __device__ __forceinline__ bool phys_recon_fast(const Prim<T>& V) {

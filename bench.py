@@ -364,9 +364,9 @@ def fp32_error_leg(E, np):
     shock-bubble to t_end (HLLC), the 512^2 adjoint case (400 steps)."""
     from large_sys_eq_opt_gb300.cases import blast_256, blast_adjoint_512, shock_bubble_1000x396
     res = {}
-    for name, prob, nsteps in (("config0_blast256_t_end", blast_256(), None),
-                               ("config1_shock_bubble_1000x396_t_end", shock_bubble_1000x396(), None),
-                               ("config3_blast512_400steps", blast_adjoint_512(), 400)):
+    for name, prob, nsteps in (("blast256_t_end", blast_256(), None),
+                               ("shock_bubble_1000x396_t_end", shock_bubble_1000x396(), None),
+                               ("blast512_400steps", blast_adjoint_512(), 400)):
         s64 = E.Solver.for_problem(prob, "fp64", "hllc")
         s64.set_dt_log(1 << 16)
         if nsteps is None:

@@ -90,7 +90,7 @@ def test_single_step_golden_cases(E, golden_dir, solver):
 
 @pytest.mark.parametrize("solver", SOLVERS)
 def test_blast256_run_to_t_end(E, port, solver):
-    """BASELINE configuration 0 geometry: 256^2 blast, CFL 0.8, t_end 0.25, 5 snapshots."""
+    """The reference's 256^2 blast case: CFL 0.8, t_end 0.25, 5 snapshots."""
     g = Grid(256, 256, 0.0, 2.0, 0.0, 2.0)
     U = port.init_blast(g)
     ref = port.run(U, g, 0.8, 0.25, solver, nsnap=5, want_snapshots=True)
@@ -112,7 +112,7 @@ def test_blast256_run_to_t_end(E, port, solver):
 
 @pytest.mark.parametrize("solver", ("hllc", "exact"))
 def test_reflective_shock_bubble(E, port, solver):
-    """BASELINE configuration 1 (1000x396, reflective y), first 0.02 of time."""
+    """The reference's 1000x396 shock-bubble case (reflective in y), first 0.02 of time."""
     g = Grid(1000, 396, 0.0, 0.225, 0.0, 0.089, bc=("transmissive", "transmissive", "reflective", "reflective"))
     U = port.init_shock_bubble(g)
     ref = port.run(U, g, 0.8, 0.02, solver)

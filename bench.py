@@ -45,6 +45,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s FP32 vs FP64 at stated L1 err vs FP64; adjoint/forward time ratio"
 UNIT = "cell-updates/s"
+REF_MAX_STEPS = 60   # reference arm: at most this many timed (and warm-up) full steps
 
 
 def parse_args():
@@ -235,12 +236,13 @@ def profiled_traffic(key: str):
     return None
 
 
-def cpu_port_rate(n: int, solver: str, seconds: float, max_steps: int | None = None):
+def cpu_port_rate(n: int, solver: str, seconds: float, max_steps: int | None = None, warmup: int = 1):
     """Oracle port (C restatement of the reference CPU solver, OpenMP on every
     host core, OMP_PROC_BIND=close OMP_PLACES=cores) on the n x n blast: the
     reference's time loop (scripts/cpu/main_cpu.cpp:221-241) with its grids
     and workspace allocated once -- per step the ghost fill, compute_dt and
-    advance_second_order -- until `seconds` of work or max_steps."""
+    advance_second_order -- `warmup` untimed steps, then until `seconds` of
+    work or max_steps."""
     import numpy as np
     os.environ.setdefault("OMP_PROC_BIND", "close")
     os.environ.setdefault("OMP_PLACES", "cores")
@@ -259,8 +261,9 @@ def cpu_port_rate(n: int, solver: str, seconds: float, max_steps: int | None = N
         dt = P.compute_dt(U, g, 0.8)
         P.advance_second_order(U, g, dt, solver, Utmp, Unew, fx, fy)
 
-    step(U, Unew)                                        # warm-up step (touches every buffer)
-    U, Unew = Unew, U
+    for _ in range(max(1, warmup)):                      # warm-up (touches every buffer)
+        step(U, Unew)
+        U, Unew = Unew, U
     steps, t0 = 0, time.perf_counter()
     while True:
         step(U, Unew)
@@ -276,14 +279,18 @@ def cpu_port_rate(n: int, solver: str, seconds: float, max_steps: int | None = N
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return
-    steps_cap = max(1, min(args.steps, 20))
-    rate, threads, steps, el = cpu_port_rate(args.n, args.solver, seconds=1e9, max_steps=steps_cap)
+    # the same K timed steps after W warm-up steps as the GPU arm, bounded so
+    # that the run stays within a few minutes (~0.9 s per full 8192^2 FP64
+    # step on 16 Grace cores)
+    steps_cap = max(1, min(args.steps, REF_MAX_STEPS))
+    warm = max(1, min(args.warmup, REF_MAX_STEPS))
+    rate, threads, steps, el = cpu_port_rate(args.n, args.solver, seconds=1e9, max_steps=steps_cap, warmup=warm)
     sample = (f"{steps} full {args.n}x{args.n} FP64 {args.solver.upper()} steps (BC + compute_dt + "
-              f"advance_second_order, grids and face caches allocated once) after 1 warm-up step, {el:.1f} s "
-              f"on {threads} threads (OMP_PROC_BIND=close OMP_PLACES=cores)")
+              f"advance_second_order, grids and face caches allocated once) after {warm} warm-up steps, "
+              f"{el:.1f} s on {threads} threads (OMP_PROC_BIND=close OMP_PLACES=cores)")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"blast_{args.n}x{args.n}_{args.solver}", "nx": args.n, "ny": args.n,
                    "solver": args.solver, "precision": "fp64 (the reference has no FP32 path)"},
@@ -360,14 +367,17 @@ def field_errors(np, got, ref):
 
 def fp32_error_leg(E, np):
     """FP32 form against FP64 per field and per configuration, both on the
-    FP64 run's dt sequence: the 256^2 blast and the 1000x396 reflective
-    shock-bubble to t_end (HLLC), the 512^2 adjoint case (400 steps)."""
+    FP64 run's dt sequence: the 256^2 blast to t_end (HLLC), the 1000x396
+    reflective shock-bubble to t_end with each of the four Riemann solvers,
+    the 512^2 adjoint case (400 steps, HLLC)."""
     from large_sys_eq_opt_gb300.cases import blast_256, blast_adjoint_512, shock_bubble_1000x396
     res = {}
-    for name, prob, nsteps in (("blast256_t_end", blast_256(), None),
-                               ("shock_bubble_1000x396_t_end", shock_bubble_1000x396(), None),
-                               ("blast512_400steps", blast_adjoint_512(), 400)):
-        s64 = E.Solver.for_problem(prob, "fp64", "hllc")
+    cases = [("blast256_t_end_hllc", blast_256(), None, "hllc")]
+    cases += [(f"shock_bubble_1000x396_t_end_{sv}", shock_bubble_1000x396(), None, sv)
+              for sv in ("hll", "hllc", "exact", "force")]
+    cases += [("blast512_400steps_hllc", blast_adjoint_512(), 400, "hllc")]
+    for name, prob, nsteps, solver in cases:
+        s64 = E.Solver.for_problem(prob, "fp64", solver)
         s64.set_dt_log(1 << 16)
         if nsteps is None:
             info = s64.run(prob.cfg.t_end)
@@ -377,12 +387,70 @@ def fp32_error_leg(E, np):
         dts = s64.dt_log(nsteps)
         ref = s64.download()
         s64.close()
-        s32 = E.Solver.for_problem(prob, "fp32", "hllc")
+        s32 = E.Solver.for_problem(prob, "fp32", solver)
         s32.step_n(nsteps, dts)
         got = s32.download()
         s32.close()
         res[name] = {"steps": int(nsteps), **field_errors(np, got, ref)}
     return res
+
+
+def developed_leg(E, np, prob, dist, t_dev=0.2):
+    """Step times on a developed flow: the 8192^2 FP32 blast is first run
+    with HLLC to t = t_dev (the ring has expanded to r ~ 0.8 and the interior
+    carries the rarefaction and contact, so few faces see identical states),
+    then HLLC and the exact solver are timed from that state (graph-replayed
+    steps, CUDA events).  Complements the early-window figures, where nearly
+    every face of the grid sees identical left and right states."""
+    cells = prob.cfg.nx * prob.cfg.ny
+    res = {"t_developed": t_dev}
+    s = E.Solver.for_problem(prob, "fp32", "hllc")
+    t0 = time.perf_counter()
+    info = s.run(t_dev)
+    res["steps_to_develop"] = int(info["steps"])
+    res["develop_wall_s"] = time.perf_counter() - t0
+    U = s.download()
+    for solver, w, k in (("hllc", 3, 50), ("exact", 3, 20)):
+        s.upload(U)
+        s.set_option("solver", {"hll": 0, "hllc": 1, "exact": 2, "force": 3}[solver])
+        s.time_steps(w)
+        s.upload(U)
+        tot, tx, ty = s.time_steps(k)
+        res[solver] = {"ms_per_step": tot / k, "value": cells * k * dist.ws / (dist.max(tot) / 1e3),
+                       "per_kernel_ms": {"sweep_x": tx / k, "sweep_y": ty / k}, "steps": k}
+    s.close()
+    return res
+
+
+def e2e_leg(E, prob, precision, solver, dist, ke=5):
+    """The metric through the drop-in call on host grids: eu_step_host
+    (Grid2D AoS in, BC + compute_dt + advance_second_order, Grid2D AoS out),
+    pinned host buffers, one warm-up step then `ke` timed steps."""
+    n = prob.cfg.nx
+    cells = prob.cfg.nx * prob.cfg.ny
+    se = E.Solver.for_problem(prob, precision, solver)
+    A = E.PinnedGrid(prob.cfg.nx, prob.cfg.ny)
+    B = E.PinnedGrid(prob.cfg.nx, prob.cfg.ny)
+    se.download(A.array)
+    t, t_end = 0.0, 1e30
+    t += se.step_host(A.array, B.array, 0.8, t, t_end)   # warm-up
+    dist.barrier()
+    t0 = time.perf_counter()
+    step_s = []
+    for k in range(ke):
+        src, dst = (B, A) if k % 2 == 0 else (A, B)
+        ts = time.perf_counter()
+        t += se.step_host(src.array, dst.array, 0.8, t, t_end)
+        step_s.append(time.perf_counter() - ts)
+    el = dist.max(time.perf_counter() - t0)
+    se.close()
+    del A, B
+    aos = (n + 4) * (prob.cfg.ny + 4) * 32
+    return {"value": cells * ke * dist.ws / el, "unit": UNIT, "h2d_bytes_per_step": aos,
+            "d2h_bytes_per_step": aos, "steps": ke, "precision": precision,
+            "call": "eu_step_host (Grid2D AoS in, BC + compute_dt + advance_second_order, AoS out)",
+            "best_step_ms": 1e3 * min(step_s), "median_step_ms": 1e3 * statistics.median(step_s),
+            "step_ms": [round(1e3 * x, 2) for x in step_s]}
 
 
 def ensemble_leg(E, np, steps=20):
@@ -542,29 +610,11 @@ def run_ours(args, dist: Dist):
         import gc
         gc.collect()
         cpus = bind_to_gpu_cpus(dist.local)
-        se = E.Solver.for_problem(prob, "fp32", args.solver)
-        A = E.PinnedGrid(n, n)
-        B = E.PinnedGrid(n, n)
-        se.download(A.array)
-        ke, t, t_end = 5, 0.0, 1e30
-        t += se.step_host(A.array, B.array, 0.8, t, t_end)   # warm-up
-        dist.barrier()
-        t0 = time.perf_counter()
-        step_s = []
-        for k in range(ke):
-            src, dst = (B, A) if k % 2 == 0 else (A, B)
-            ts = time.perf_counter()
-            t += se.step_host(src.array, dst.array, 0.8, t, t_end)
-            step_s.append(time.perf_counter() - ts)
-        el = dist.max(time.perf_counter() - t0)
-        aos = (n + 4) * (n + 4) * 32
-        out["e2e"] = {"value": cells * ke * dist.ws / el, "unit": UNIT, "h2d_bytes_per_step": aos,
-                      "d2h_bytes_per_step": aos, "steps": ke,
-                      "call": "eu_step_host (Grid2D AoS in, BC + compute_dt + advance_second_order, AoS out)",
-                      "host_cpus": cpus, "best_step_ms": 1e3 * min(step_s), "median_step_ms": 1e3 * statistics.median(step_s),
-                      "step_ms": [round(1e3 * x, 2) for x in step_s]}
-        se.close()
-        del A, B
+        out["e2e"] = e2e_leg(E, prob, "fp32", args.solver, dist)
+        out["e2e"]["host_cpus"] = cpus
+        gc.collect()
+        # the like-for-like drop-in figure: FP64 arithmetic, as the reference
+        out["e2e_fp64"] = e2e_leg(E, prob, "fp64", args.solver, dist)
 
     # ---- FP64 throughput + FP32-vs-FP64 error at the final step -----------
     if not args.skip_fp64:
@@ -574,6 +624,10 @@ def run_ours(args, dist: Dist):
     # ---- the other Riemann solvers on the same grid ------------------------
     if not args.skip_solvers:
         out["solvers"] = solvers_leg(E, np, prob, dist)
+
+    # ---- developed-flow step times (FP32 HLLC and exact) -------------------
+    if not args.skip_solvers:
+        out["developed"] = developed_leg(E, np, prob, dist)
 
     # ---- discrete adjoint: time ratio against the forward -----------------
     if not args.skip_adjoint:
@@ -614,6 +668,25 @@ def run_ours(args, dist: Dist):
                                       if "adjoint" in out else None),
         }
         line.update(out)
+        # the headline figures once more at the end of the line (the part a
+        # truncated log keeps): FP32 and FP64, device-resident and e2e, and
+        # the CPU baseline they compare with
+        summ = {"fp32_value": value, "fp32_e2e": out.get("e2e", {}).get("value"),
+                "fp64_value": out.get("fp64", {}).get("value"), "fp64_e2e": out.get("e2e_fp64", {}).get("value"),
+                "cpu_baseline_fp64": out.get("cpu_baseline", {}).get("value"),
+                "roofline_frac": out["roofline"]["frac"], "roofline_kernel": out["roofline"]["kernel"]}
+        cb = summ["cpu_baseline_fp64"]
+        for k in ("fp32_value", "fp32_e2e", "fp64_value", "fp64_e2e"):
+            if cb and summ[k]:
+                summ[k + "_over_cpu"] = summ[k] / cb
+        if summ["fp64_value"]:
+            summ["fp32_over_fp64"] = value / summ["fp64_value"]
+        if "adjoint" in out:
+            summ["adjoint_backward_over_forward"] = {p: out["adjoint"][p]["backward_over_forward"]
+                                                     for p in ("fp32", "fp64")}
+        if "fp32_error_by_config" in out:
+            summ["fp32_l1_rho_by_config"] = {k: v["rho"]["l1"] for k, v in out["fp32_error_by_config"].items()}
+        line["summary"] = summ
         print(json.dumps(line), flush=True)
 
 

@@ -158,11 +158,16 @@ int eu_totals(eu_handle* h, double out[4]);
  *           reaches it.
  * Scratch: a fixed 1 MiB array inside the library (8 doubles per interior
  * row).  ny > 16384 is rejected with EU_ERR_INVALID; nothing in the scratch
- * has to start at zero.  The first call on each device (with that device
- * current) looks the scratch up with cudaGetSymbolAddress: make it before any
- * stream capture begins.  All calls on one device share the scratch, so two
- * calls whose work overlaps (different streams or host threads, unordered)
- * race and give wrong totals: order them on one stream or with events. */
+ * has to start at zero.  Every call looks the scratch's address up with
+ * cudaGetSymbolAddress in the current context (so a device reset cannot
+ * leave a stale address).  With lazy module loading, the CUDA default, the
+ * first call on a device loads the library's device image, 1 MiB array
+ * included: that one call may take device memory.  A caller that hands all
+ * HBM to its own pool makes one warm-up call first (or sets
+ * CUDA_MODULE_LOADING=EAGER), and makes the first call before any stream
+ * capture begins.  All calls on one device share the scratch, so two calls
+ * whose work overlaps (different streams or host threads, unordered) race
+ * and give wrong totals: order them on one stream or with events. */
 int eu_totals_noalloc(const double* d_aos, int nx, int ny, double* d_out, void* stream);
 
 /* ---- discrete adjoint (no counterpart in the reference) ---------------------- */
@@ -252,7 +257,12 @@ void eu_host_free(void* p);
  * (x-sweep segment length, a multiple of the box width), "seg_y" (y-sweep
  * rows per warp), "l2_promotion_x" / "l2_promotion_y" (TMA L2 promotion in
  * bytes: 0, 64, 128, 256; defaults 128 and 256), "graph_steps" (steps per
- * replayed graph).
+ * replayed graph), "solver" (the eu_solver of later steps: the reference
+ * passes the solver to every advance_second_order call,
+ * head/cpu/solver_cpu.hpp:62-80, so one handle serves every solver of a
+ * geometry; the state is kept, the launch plan becomes the planner's for the
+ * new solver; an adjoint backward pass uses the solver of its forward pass,
+ * and a batch's own ensemble steps keep the batch's solver).
  * Read-only: "tasks_x", "tasks_y".  Used by the tile-shape autotuner. */
 int eu_set_option(eu_handle* h, const char* name, long long value);
 int eu_get_option(eu_handle* h, const char* name, long long* value);

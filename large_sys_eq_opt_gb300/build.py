@@ -99,7 +99,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     objs = [os.path.join(BUILD, obj) for _, obj, _ in units()]
     tmp = LIB + ".tmp"
-    link = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"] * 0
+    link = [cc] + ARCH + ["-shared", "-o", tmp] + objs
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + " ".join(link) + "\n" + r.stdout + r.stderr)

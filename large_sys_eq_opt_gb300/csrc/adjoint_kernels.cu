@@ -10,6 +10,7 @@
 // states of a checkpoint segment sit in L2.
 #include "adjoint.cuh"
 #include "adjoint_kernels.h"
+#include "per_device.h"
 
 #ifndef EU_PREC
 #error "EU_PREC (32 or 64) must be defined"
@@ -105,7 +106,9 @@ template <int DIR, int NL, int TC> cudaError_t launch(const AdjSweepArgs& a, cud
     acc.bc_hi = a.bc_hi;
     constexpr size_t smem = sizeof(adj::TileMem<T, NL, TC>);
     auto k = adjoint_sweep_kernel<DIR, NL, TC>;
-    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static PerDevice<cudaError_t> attr_cache;
+    const cudaError_t attr = attr_cache.get(
+        [k] { return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
     if (attr != cudaSuccess) return attr;
     const long long ctas = (long long)((acc.nlines + NL - 1) / NL) * ((acc.n + TC - 1) / TC);
     k<<<(unsigned)ctas, kThreads, smem, s>>>(acc);

@@ -643,6 +643,20 @@ int eu_set_option(eu_handle* h, const char* name, long long value) {
     } else if (k == "graph_steps") {
         if (value < 1 || value > 4096) return fail(h, EU_ERR_INVALID, "graph_steps must be in [1, 4096]");
         h->gsteps = (int)value;
+    } else if (k == "solver") {
+        // the Riemann solver of later steps (the reference passes it per
+        // call, src/cpu/solver_cpu.cpp:400-405); the state is kept and the
+        // launch plan is the planner's for the new solver
+        if (value < EU_HLL || value > EU_FORCE) return fail(h, EU_ERR_INVALID, "solver must be 0..3");
+        if (value != h->solver) {
+            if (cudaStreamSynchronize(h->st) != cudaSuccess) {
+                (void)cudaGetLastError();
+                return fail(h, EU_ERR_CUDA, "eu_set_option(solver): stream synchronisation failed");
+            }
+            h->solver = (int)value;
+            h->K = kernels_for(h->prec, h->solver);
+            plan(h);
+        }
     } else {
         return fail(h, EU_ERR_INVALID, "unknown option " + k);
     }
@@ -658,6 +672,7 @@ int eu_get_option(eu_handle* h, const char* name, long long* value) {
     else if (k == "seg_x") *value = h->seg_x;
     else if (k == "seg_y") *value = h->seg_y;
     else if (k == "graph_steps") *value = h->gsteps;
+    else if (k == "solver") *value = h->solver;
     else if (k == "tasks_x") *value = h->ntasks_x;
     else if (k == "occ_x") *value = h->K.occ_x();
     else if (k == "occ_y") *value = h->K.occ_y();

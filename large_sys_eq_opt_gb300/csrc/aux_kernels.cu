@@ -3,6 +3,7 @@
 // the standalone CFL reduction (first step / compute_dt), FP64 audits of the
 // conserved totals, snapshot unpacking.
 #include "aux_kernels.h"
+#include "per_device.h"
 #include "sweeps.cuh"
 
 namespace eu {
@@ -240,7 +241,8 @@ __global__ void totals_final_kernel(const double* part, int nblocks, double* out
 // ---------------------------------------------------------------------------
 static int grid_for(long long n, int threads) {
     long long b = (n + threads - 1) / threads;
-    if (b > 152LL * 16) b = 152LL * 16;
+    const long long cap = 16LL * sm_count_current();   // grid-stride loops: 16 CTAs per SM at most
+    if (b > cap) b = cap;
     return (int)(b < 1 ? 1 : b);
 }
 

@@ -17,11 +17,18 @@
 //   * divisions by constants and repeated divisions by the same value become
 //     multiplications by a reciprocal;
 //   * the FP32 form (T = float) runs in single precision with approximate
-//     reciprocal / square root, and keeps FP64 in two places: pressure
-//     recovery p = (gamma-1)(E - rho|u|^2/2) whenever the kinetic energy
-//     exceeds half the total energy (there the FP32 subtraction would lose
-//     more than one bit to cancellation), and the exact solver's Newton
-//     iteration for p*, which runs entirely in FP64.
+//     reciprocal / square root, and keeps FP64 in two places, each of them
+//     conditional (a deviation from an unconditional FP64 island, stated
+//     with the FP32 error figures):
+//       - pressure recovery p = (gamma-1)(E - rho|u|^2/2) is redone in FP64
+//         only when the kinetic energy exceeds half the total energy (there
+//         the FP32 subtraction would lose more than one bit to
+//         cancellation; below it loses at most one);
+//       - the exact solver's p*: Newton's iteration runs in FP32 to a
+//         relative step of 1e-5 and is finished by one FP64 Newton step
+//         (exact_star_mixed); irregular cases (non-positive iterate, no
+//         convergence in 12 steps, tiny f', a large FP64 step) run the full
+//         FP64 iteration.  The FP64 form keeps the reference's iteration.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>

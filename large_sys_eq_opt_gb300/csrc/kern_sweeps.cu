@@ -3,6 +3,7 @@
 // eight variants build in parallel; the Riemann solver is a template
 // parameter, never a per-face runtime switch.
 #include "aux_kernels.h"
+#include "per_device.h"
 #include "sweeps.cuh"
 
 #ifndef EU_PREC
@@ -52,7 +53,9 @@ constexpr size_t kSmemY = 1024 + NW * (SY * kStageY + 2 * kOStageY) + NW * SY * 
 static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args, int ctas,
                             cudaStream_t s) {
     auto k = sweep_x_kernel<T, SOL, SX, NW, MINB_X>;
-    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX);
+    static PerDevice<cudaError_t> attr_cache;
+    const cudaError_t attr = attr_cache.get(
+        [k] { return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemX); });
     if (attr != cudaSuccess) return attr;
     k<<<ctas, NW * 32, kSmemX, s>>>(*tm, *tm_out, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
@@ -61,17 +64,20 @@ static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, co
 static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args, int ctas,
                             cudaStream_t s) {
     auto k = sweep_y_kernel<T, SOL, RY, BWY, SY, NW, MINB_Y>;
-    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY);
+    static PerDevice<cudaError_t> attr_cache;
+    const cudaError_t attr = attr_cache.get(
+        [k] { return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemY); });
     if (attr != cudaSuccess) return attr;
     // persistent: at most one CTA per resident slot (the warps share the work list)
-    static const int slots = [k]() {
-        int dev = 0, sms = 0, occ = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            sms = 1;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, NW * 32, kSmemY) != cudaSuccess || occ < 1) occ = 1;
-        return sms * occ;
-    }();
+    static PerDevice<int> slot_cache;
+    const int slots = slot_cache.get([k]() {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, NW * 32, kSmemY) != cudaSuccess || occ < 1) {
+            (void)cudaGetLastError();
+            occ = 1;
+        }
+        return sm_count_current() * occ;
+    });
     k<<<ctas < slots ? ctas : slots, NW * 32, kSmemY, s>>>(*tm, *tm_out, *static_cast<const SweepArgs<T>*>(args));
     return cudaGetLastError();
 }
@@ -79,7 +85,8 @@ static cudaError_t LAUNCH_Y(const CUtensorMap* tm, const CUtensorMap* tm_out, co
 static cudaError_t LAUNCH_F(const void* in, const void* out, int nx, int ny, double dtdx, double dtdy,
                             cudaStream_t s) {
     long long blocks = ((long long)nx * ny + 255) / 256;
-    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    const long long cap = 32LL * sm_count_current();   // grid-stride loop: 32 CTAs per SM at most
+    if (blocks > cap) blocks = cap;
     first_order_kernel<T, SOL><<<(int)blocks, 256, 0, s>>>(*static_cast<const Planes<T>*>(in),
                                                            *static_cast<const Planes<T>*>(out), nx, ny, dtdx, dtdy);
     return cudaGetLastError();
@@ -89,7 +96,9 @@ constexpr size_t kSmemE = ensemble_smem<T, SX, RY, BWY, SY, NW>();
 
 static cudaError_t LAUNCH_E(const void* args, int ctas, cudaStream_t s) {
     auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_Y>;
-    static const cudaError_t attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemE);
+    static PerDevice<cudaError_t> attr_cache;
+    const cudaError_t attr = attr_cache.get(
+        [k] { return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemE); });
     if (attr != cudaSuccess) return attr;
     k<<<ctas, NW * 32, kSmemE, s>>>(*static_cast<const EnsArgs<T>*>(args));
     return cudaGetLastError();

@@ -17,9 +17,19 @@
 // with EU_ERR_INVALID.  Nothing in the scratch has to start at zero: pass 1
 // writes the slots of rows 0..ny-1 before pass 2 reads exactly those slots.
 //
-// Set-up: the first call on each device (with that device current) looks up
-// the scratch address with cudaGetSymbolAddress and keeps it; later calls on
-// that device reuse it.  Make that first call before any stream capture
+// Set-up: every call looks the scratch address up with cudaGetSymbolAddress,
+// with the calling thread's current device current, checks the result and
+// passes that address to the kernels.  The host-side name g_row_part is only
+// a stand-in for the device array and is never handed to a kernel.  The
+// lookup is repeated on every call instead of being cached, because after a
+// cudaDeviceReset (or any re-creation of the primary context) the library's
+// device image is loaded again, possibly at another address, and a cached
+// address would make the kernels write through a stale pointer.  With lazy
+// module loading (the CUDA default) the first call on a device also loads
+// this library's device image, including the 1 MiB array, so that first
+// call may take device memory once; callers that hand all HBM to their own
+// pool should make one warm-up call (or set CUDA_MODULE_LOADING=EAGER)
+// before they reserve it, and make the first call before any stream capture
 // begins.
 //
 // Concurrency: every call on one device uses the same scratch.  Two calls
@@ -30,7 +40,6 @@
 
 #include <cmath>
 #include <cstdint>
-#include <mutex>
 
 #include "../../include/euler2d.h"
 
@@ -41,7 +50,6 @@ void set_global_error(const char* msg);
 namespace {
 
 constexpr int kNoallocMaxRows = 16384;
-constexpr int kMaxDevices = 64;
 constexpr int kRowsPerBlock = 8;  // one warp per interior row
 
 // Row partials: row j's Neumaier sum of field f at [8j + f], its
@@ -115,9 +123,6 @@ __global__ void __launch_bounds__(256) noalloc_fold_kernel(const double* __restr
     }
 }
 
-std::mutex g_setup_mu;
-double* g_scratch[kMaxDevices] = {};
-
 int fail(int code, const char* msg) {
     eu::set_global_error(msg);
     return code;
@@ -146,26 +151,20 @@ extern "C" int eu_totals_noalloc(const double* d_aos, int nx, int ny, double* d_
     if ((reinterpret_cast<uintptr_t>(d_aos) & 15u) || (reinterpret_cast<uintptr_t>(d_out) & 7u))
         return fail(EU_ERR_INVALID, "eu_totals_noalloc: d_aos must be 16-byte and d_out 8-byte aligned");
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
         (void)cudaGetLastError();
         return fail(EU_ERR_CUDA, "eu_totals_noalloc: no usable current CUDA device");
     }
     if (!on_device(d_aos, dev) || !on_device(d_out, dev))
         return fail(EU_ERR_INVALID, "eu_totals_noalloc: d_aos and d_out must be device memory of the current device");
-    double* scratch;
-    {
-        std::lock_guard<std::mutex> g(g_setup_mu);
-        if (!g_scratch[dev]) {
-            void* p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_row_part);
-            if (e != cudaSuccess || !p) {
-                (void)cudaGetLastError();
-                return fail(EU_ERR_CUDA, "eu_totals_noalloc: cudaGetSymbolAddress of the scratch failed");
-            }
-            g_scratch[dev] = static_cast<double*>(p);
-        }
-        scratch = g_scratch[dev];
+    // the scratch's device address in the current context (see the header)
+    void* p = nullptr;
+    const cudaError_t le = cudaGetSymbolAddress(&p, g_row_part);
+    if (le != cudaSuccess || !p) {
+        (void)cudaGetLastError();
+        return fail(EU_ERR_CUDA, "eu_totals_noalloc: cudaGetSymbolAddress of the scratch failed");
     }
+    double* scratch = static_cast<double*>(p);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int blocks = (ny + kRowsPerBlock - 1) / kRowsPerBlock;
     noalloc_rows_kernel<<<blocks, 32 * kRowsPerBlock, 0, s>>>(d_aos, nx, ny, scratch);

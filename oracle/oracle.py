@@ -24,7 +24,24 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle_euler2d.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_euler2d.so")
-REFERENCE_TREE = "/root/reference"
+
+
+def _reference_tree() -> str:
+    """Location of the reference sources: $EULER2D_REFERENCE when set, else
+    the REF default of oracle/Makefile (the recipe that compiles them where
+    they lie).  An empty string when neither names a directory."""
+    env = os.environ.get("EULER2D_REFERENCE")
+    if env:
+        return env
+    try:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "refdir"],
+                           capture_output=True, text=True, timeout=30)
+        return r.stdout.strip() if r.returncode == 0 else ""
+    except (OSError, subprocess.SubprocessError):
+        return ""
+
+
+REFERENCE_TREE = _reference_tree()
 
 SOLVERS = {"hll": 0, "hllc": 1, "exact": 2, "force": 3}
 BC = {"transmissive": 0, "reflective": 1}
@@ -44,9 +61,9 @@ def build(reference: bool | None = None) -> None:
     """Compile the restatement (always) and the reference harness (when the
     reference tree exists or ``reference`` is True)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    want_ref = os.path.isdir(REFERENCE_TREE) if reference is None else reference
+    want_ref = bool(REFERENCE_TREE) and os.path.isdir(REFERENCE_TREE) if reference is None else reference
     if want_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True,
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_TREE}"], check=True,
                        stderr=subprocess.DEVNULL)
 
 

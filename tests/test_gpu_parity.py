@@ -110,18 +110,39 @@ def test_blast256_run_to_t_end(E, port, solver):
     assert l1(interior(got)[..., 0], interior(U)[..., 0]) <= 1e-10
 
 
-@pytest.mark.parametrize("solver", ("hllc", "exact"))
-def test_reflective_shock_bubble(E, port, solver):
-    """The reference's 1000x396 shock-bubble case (reflective in y), first 0.02 of time."""
+@pytest.mark.parametrize("solver", SOLVERS)
+def test_reflective_shock_bubble_to_t_end(E, port, solver):
+    """The 1000x396 single-gas shock-bubble (Mach 1.22 shock, bubble rho 0.138,
+    transmissive in x, reflective in y, CFL 0.8) run to t_end = 0.1 with each
+    Riemann solver: the FP64 path against the oracle (equal step count and
+    snapshot steps, L1(rho) <= 1e-10 at t_end, the other fields reported and
+    held to 1e-9), and the FP32 form on the FP64 dt sequence (L1(rho) <= 1e-5
+    against the FP64 oracle, the FP32 form's bar)."""
     g = Grid(1000, 396, 0.0, 0.225, 0.0, 0.089, bc=("transmissive", "transmissive", "reflective", "reflective"))
     U = port.init_shock_bubble(g)
-    ref = port.run(U, g, 0.8, 0.02, solver)
-    with E.Solver(cfg_of(g, 0.8, 0.02), "fp64", solver, bc=bc_of(g)) as s:
+    ref = port.run(U, g, 0.8, 0.1, solver, nsnap=5, want_snapshots=False)
+    snaps = {}
+    with E.Solver(cfg_of(g, 0.8, 0.1), "fp64", solver, bc=bc_of(g)) as s:
         s._check(s._L.eu_init_shock_bubble(s._h, 1.0, 1.0, 1.22, 0.005, 0.035, 0.0445, 0.025, 0.138))
-        info = s.run(0.02)
+        s.set_dt_log(1 << 14)
+        info = s.run(0.1, nsnap=5, callback=lambda k, step, t, A: snaps.__setitem__(k, (step, t)))
         got = s.download()
+        dts = s.dt_log(info["steps"])
     assert info["steps"] == ref["steps"]
-    assert l1(interior(got)[..., 0], interior(U)[..., 0]) <= 1e-10
+    assert abs(info["t"] - ref["t"]) <= 1e-15
+    for k in range(5):
+        assert snaps[k + 1][0] == ref["snap_step"][k]
+        assert abs(snaps[k + 1][1] - ref["snap_t"][k]) <= 1e-14
+    errs = [l1(interior(got)[..., f], interior(U)[..., f]) for f in range(4)]
+    assert errs[0] <= 1e-10, (solver, errs)
+    assert max(errs) <= 1e-9, (solver, errs)
+    with E.Solver(cfg_of(g, 0.8, 0.1), "fp32", solver, bc=bc_of(g)) as s:
+        s._check(s._L.eu_init_shock_bubble(s._h, 1.0, 1.0, 1.22, 0.005, 0.035, 0.0445, 0.025, 0.138))
+        s.step_n(len(dts), dts)
+        got32 = s.download()
+    e32 = l1(interior(got32)[..., 0], interior(U)[..., 0])
+    assert e32 <= 1e-5, (solver, e32)
+    print(f"shock-bubble {solver}: {ref['steps']} steps, FP64 L1 per field {errs}, FP32 L1(rho) {e32:.3e}")
 
 
 @pytest.mark.parametrize("shape", [(17, 13), (1, 24), (24, 1), (130, 5), (5, 131), (1, 1), (2, 2), (3, 1)])

@@ -77,3 +77,39 @@ def test_noalloc_rejects_bad_arguments(E):
     assert L.eu_totals_noalloc(dev.data_ptr() + 8, 1, 4, out.data_ptr(), None) == 1
     assert L.eu_totals_noalloc(None, 1, 4, out.data_ptr(), None) == 1
     assert L.eu_totals_noalloc(dev.data_ptr(), 0, 4, out.data_ptr(), None) == 1
+    # d_out given as a host pointer (pinned or pageable) is rejected too
+    assert L.eu_totals_noalloc(dev.data_ptr(), 1, 4, host.ctypes.data_as(C.c_void_p), None) == 1
+    assert b"device memory" in L.eu_last_error(None)
+
+
+def test_noalloc_accepts_managed_memory_and_8_byte_aligned_output(E, port):
+    """Managed (unified) memory passes the pointer checks, and d_out needs
+    only 8-byte alignment: the totals land in the second double of a
+    managed buffer, equal to eu_totals on a handle."""
+    import torch
+    try:
+        cu = C.CDLL("libcuda.so.1")
+    except OSError:
+        pytest.skip("libcuda.so.1 not loadable")
+    nx, ny = 64, 40
+    g = Grid(nx, ny, 0.0, 2.0, 0.0, 2.0)
+    U = port.init_blast(g, cx=1.1, cy=0.9, r=0.5)
+    ref = handle_totals(E, g, U)
+    torch.cuda.synchronize()        # torch's primary context is current on this thread
+    nbytes = U.nbytes + 64
+    ptr = C.c_uint64(0)
+    assert cu.cuMemAllocManaged(C.byref(ptr), C.c_size_t(nbytes), C.c_uint(1)) == 0   # CU_MEM_ATTACH_GLOBAL
+    try:
+        base = ptr.value
+        out_addr = base + U.nbytes + 8          # 8-byte but not 16-byte aligned
+        assert out_addr % 16 == 8
+        C.memmove(C.c_void_p(base), U.ctypes.data_as(C.c_void_p), U.nbytes)
+        L = E.load()
+        assert L.eu_totals_noalloc(base, nx, ny, out_addr, None) == 0, L.eu_last_error(None)
+        torch.cuda.synchronize()
+        got = np.frombuffer((C.c_double * 4).from_address(out_addr), dtype=np.float64).copy()
+        scale = np.abs(U[2:-2, 2:-2]).sum(axis=(0, 1))
+        assert np.all(np.abs(got - ref) <= 1e-14 * scale + 1e-300), (got, ref)
+    finally:
+        torch.cuda.synchronize()
+        assert cu.cuMemFree_v2(ptr) == 0

@@ -425,19 +425,21 @@ int orc_get_threads(void) {
 /* head/cpu/boundary_cpu.hpp:5-37, generalised: each ghost layer g copies the
  * nearest interior cell (transmissive) or mirrors cell g with the normal
  * momentum negated (reflective).  x pass over interior rows, then y pass
- * over every column so corners take the y rule of the x ghosts. */
+ * over every column so corners take the y rule of the x ghosts.  A side of
+ * kind ORC_BC_HALO (an internal side of a sub-domain) is left untouched: its
+ * ghosts are a neighbour's cells, filled by a halo exchange. */
 void orc_apply_boundary(double* U, const orc_grid* g) {
     const int ib = NG, ie = NG + g->nx, jb = NG, je = NG + g->ny;
     const int total_nx = (int)tnx(g);
     for (int j = jb; j < je; ++j) {
-        for (int k = 0; k < NG; ++k) {
+        for (int k = 0; k < NG && g->bc[0] != ORC_BC_HALO; ++k) {
             if (g->bc[0] == ORC_BC_REFLECTIVE) {
                 cons_t s = ld(U, g, ib + k, j); s.rhou = -s.rhou; st(U, g, ib - 1 - k, j, s);
             } else {
                 st(U, g, ib - 1 - k, j, ld(U, g, ib, j));
             }
         }
-        for (int k = 0; k < NG; ++k) {
+        for (int k = 0; k < NG && g->bc[1] != ORC_BC_HALO; ++k) {
             if (g->bc[1] == ORC_BC_REFLECTIVE) {
                 cons_t s = ld(U, g, ie - 1 - k, j); s.rhou = -s.rhou; st(U, g, ie + k, j, s);
             } else {
@@ -446,14 +448,14 @@ void orc_apply_boundary(double* U, const orc_grid* g) {
         }
     }
     for (int i = 0; i < total_nx; ++i) {
-        for (int k = 0; k < NG; ++k) {
+        for (int k = 0; k < NG && g->bc[2] != ORC_BC_HALO; ++k) {
             if (g->bc[2] == ORC_BC_REFLECTIVE) {
                 cons_t s = ld(U, g, i, jb + k); s.rhov = -s.rhov; st(U, g, i, jb - 1 - k, s);
             } else {
                 st(U, g, i, jb - 1 - k, ld(U, g, i, jb));
             }
         }
-        for (int k = 0; k < NG; ++k) {
+        for (int k = 0; k < NG && g->bc[3] != ORC_BC_HALO; ++k) {
             if (g->bc[3] == ORC_BC_REFLECTIVE) {
                 cons_t s = ld(U, g, i, je - 1 - k); s.rhov = -s.rhov; st(U, g, i, je + k, s);
             } else {
@@ -503,23 +505,18 @@ static inline cons_t muscl_flux_y(const double* U, const orc_grid* g, int i, int
     return riemann_flux(a_r, b_l, ORC_DIR_Y, solver);
 }
 
-/* src/cpu/solver_cpu.cpp:400-499 (plus the BC hook at :461 and :498) */
-void orc_advance_second_order(const double* Uold, double* Utmp, double* Unew,
-                              const orc_grid* g, double dt, int solver,
-                              double* fx, double* fy) {
+/* The x half of src/cpu/solver_cpu.cpp:400-499: fill_x_face_cache
+ * (:206-238) and the x update (:437-457) of Utmp's interior from Uold; no
+ * ghost fill.  fx: 4*(nx+1)*ny doubles or NULL. */
+void orc_sweep_x(const double* Uold, double* Utmp, const orc_grid* g, double dt, int solver, double* fx) {
     const int ib = NG, ie = NG + g->nx, jb = NG, je = NG + g->ny;
     const int nx = g->nx, ny = g->ny;
     const int nx_faces = nx + 1;
     double* fx_own = NULL;
-    double* fy_own = NULL;
     if (!fx) fx = fx_own = (double*)malloc(sizeof(double) * 4 * (size_t)(nx + 1) * ny);
-    if (!fy) fy = fy_own = (double*)malloc(sizeof(double) * 4 * (size_t)nx * (ny + 1));
     const double dt_over_dx = dt / gdx(g);
-    const double dt_over_dy = dt / gdy(g);
-
-    /* fill_x_face_cache, src/cpu/solver_cpu.cpp:206-238 (dt/dx recomputed there) */
     {
-        const double lam = dt / gdx(g);
+        const double lam = dt / gdx(g);   /* recomputed in fill_x_face_cache */
 #ifdef _OPENMP
 #pragma omp parallel for collapse(2) schedule(static)
 #endif
@@ -541,9 +538,18 @@ void orc_advance_second_order(const double* Uold, double* Utmp, double* Unew,
             const cons_t Fp = c_make(pp[0], pp[1], pp[2], pp[3]);
             st(Utmp, g, i, j, c_sub(ld(Uold, g, i, j), c_scale(dt_over_dx, c_sub(Fp, Fm))));
         }
-    orc_apply_boundary(Utmp, g);
+    free(fx_own);
+}
 
-    /* fill_y_face_cache, src/cpu/solver_cpu.cpp:247-279 */
+/* The y half: fill_y_face_cache (src/cpu/solver_cpu.cpp:247-279) and the y
+ * update (:474-494) of Unew's interior from Utmp (ghost rows included in
+ * its stencil); no ghost fill.  fy: 4*nx*(ny+1) doubles or NULL. */
+void orc_sweep_y(const double* Utmp, double* Unew, const orc_grid* g, double dt, int solver, double* fy) {
+    const int ib = NG, ie = NG + g->nx, jb = NG, je = NG + g->ny;
+    const int nx = g->nx, ny = g->ny;
+    double* fy_own = NULL;
+    if (!fy) fy = fy_own = (double*)malloc(sizeof(double) * 4 * (size_t)nx * (ny + 1));
+    const double dt_over_dy = dt / gdy(g);
     {
         const double lam = dt / gdy(g);
 #ifdef _OPENMP
@@ -567,9 +573,17 @@ void orc_advance_second_order(const double* Uold, double* Utmp, double* Unew,
             const cons_t Fp = c_make(pp[0], pp[1], pp[2], pp[3]);
             st(Unew, g, i, j, c_sub(ld(Utmp, g, i, j), c_scale(dt_over_dy, c_sub(Fp, Fm))));
         }
-    orc_apply_boundary(Unew, g);
-    free(fx_own);
     free(fy_own);
+}
+
+/* src/cpu/solver_cpu.cpp:400-499 (plus the BC hook at :461 and :498) */
+void orc_advance_second_order(const double* Uold, double* Utmp, double* Unew,
+                              const orc_grid* g, double dt, int solver,
+                              double* fx, double* fy) {
+    orc_sweep_x(Uold, Utmp, g, dt, solver, fx);
+    orc_apply_boundary(Utmp, g);
+    orc_sweep_y(Utmp, Unew, g, dt, solver, fy);
+    orc_apply_boundary(Unew, g);
 }
 
 /* src/cpu/solver_cpu.cpp:315-369 */

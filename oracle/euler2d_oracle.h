@@ -31,7 +31,7 @@ extern "C" {
 #endif
 
 enum { ORC_HLL = 0, ORC_HLLC = 1, ORC_EXACT = 2, ORC_FORCE = 3 };
-enum { ORC_BC_TRANSMISSIVE = 0, ORC_BC_REFLECTIVE = 1 };
+enum { ORC_BC_TRANSMISSIVE = 0, ORC_BC_REFLECTIVE = 1, ORC_BC_HALO = 2 };
 enum { ORC_DIR_X = 0, ORC_DIR_Y = 1 };
 
 typedef struct {
@@ -46,7 +46,8 @@ long long orc_grid_doubles(const orc_grid* g);
 void orc_set_threads(int n);
 int orc_get_threads(void);
 
-/* Ghost fill (head/cpu/boundary_cpu.hpp:5-37 generalised per side). */
+/* Ghost fill (head/cpu/boundary_cpu.hpp:5-37 generalised per side;
+ * ORC_BC_HALO sides are left to a halo exchange). */
 void orc_apply_boundary(double* U, const orc_grid* g);
 
 /* CFL step (src/cpu/solver_cpu.cpp:287-309).  Returns 0 and writes *dt,
@@ -61,6 +62,13 @@ int orc_compute_dt(const double* U, const orc_grid* g, double cfl, double* dt);
 void orc_advance_second_order(const double* Uold, double* Utmp, double* Unew,
                               const orc_grid* g, double dt, int solver,
                               double* fx, double* fy);
+
+/* The two halves of orc_advance_second_order without its ghost fills, for a
+ * sub-domain stepper that exchanges halo rows between them: the x-sweep
+ * Uold -> Utmp interior, and the y-sweep Utmp (ghost rows included) -> Unew
+ * interior.  fx / fy as above, or NULL. */
+void orc_sweep_x(const double* Uold, double* Utmp, const orc_grid* g, double dt, int solver, double* fx);
+void orc_sweep_y(const double* Utmp, double* Unew, const orc_grid* g, double dt, int solver, double* fy);
 
 /* First-order Godunov step (src/cpu/solver_cpu.cpp:315-369). */
 void orc_advance_first_order(const double* Uold, double* Unew,

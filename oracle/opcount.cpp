@@ -62,6 +62,8 @@ inline bool isfinite(Counted a) { ++opc::g_count[opc::kCmp]; return std::isfinit
 #define orc_compute_dt opc_compute_dt_
 #define orc_advance_second_order opc_advance_second_order_
 #define orc_advance_first_order opc_advance_first_order_
+#define orc_sweep_x opc_sweep_x_
+#define orc_sweep_y opc_sweep_y_
 #define orc_riemann_flux opc_riemann_flux_
 #define orc_run opc_run_
 #define orc_init_reference_case opc_init_reference_case_

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import shutil
 import subprocess
 
 import numpy as np
@@ -44,7 +45,7 @@ def _reference_tree() -> str:
 REFERENCE_TREE = _reference_tree()
 
 SOLVERS = {"hll": 0, "hllc": 1, "exact": 2, "force": 3}
-BC = {"transmissive": 0, "reflective": 1}
+BC = {"transmissive": 0, "reflective": 1, "halo": 2}
 
 _dp = C.POINTER(C.c_double)
 _llp = C.POINTER(C.c_longlong)
@@ -58,9 +59,16 @@ class OrcGrid(C.Structure):
 
 
 def build(reference: bool | None = None) -> None:
-    """Compile the restatement (always) and the reference harness (when the
-    reference tree exists or ``reference`` is True)."""
+    """Compile the restatement (always), the loader of the reference's GPU
+    image (where nvcc is), and the reference CPU build plus the reference's
+    GPU device image (when the reference tree exists or ``reference`` is
+    True)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc"):
+        env = dict(os.environ)
+        if not shutil.which("nvcc"):
+            env["NVCC"] = "/usr/local/cuda/bin/nvcc"
+        subprocess.run(["make", "-s", "-C", HERE, "refgpu_harness"], check=True, env=env)
     want_ref = bool(REFERENCE_TREE) and os.path.isdir(REFERENCE_TREE) if reference is None else reference
     if want_ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_TREE}"], check=True,
@@ -68,6 +76,74 @@ def build(reference: bool | None = None) -> None:
 
 
 OPC_SO = os.path.join(HERE, "_build", "libopcount_euler2d.so")
+REFGPU_SO = os.path.join(HERE, "_build", "libref_gpu_harness.so")
+REFGPU_IMAGE = os.path.join(HERE, "_ref", "ref_solver_gpu.cubin")
+
+
+def reference_gpu_available() -> bool:
+    """The reference's own GPU device image and its loader are both built."""
+    return os.path.exists(REFGPU_SO) and os.path.exists(REFGPU_IMAGE)
+
+
+def reference_gpu_run(U: np.ndarray, g: "Grid", solver="hllc", cfl=0.8, warmup=0, nsteps=1):
+    """The reference's own CUDA kernels (src/gpu/solver_gpu.cu, unmodified,
+    compiled into oracle/_ref/ref_solver_gpu.cubin) stepped by the loop of
+    scripts/gpu/main_gpu.cu (oracle/ref_gpu_harness.cu): `warmup` untimed and
+    `nsteps` timed free CFL steps from U, which is advanced in place.
+    Transmissive boundaries only (the reference kernels clamp their
+    stencils).  Returns dict(wall_ms, dt_ms, x_ms, y_ms, dts) over the timed
+    steps."""
+    lib = C.CDLL(REFGPU_SO)
+    lib.refgpu_last_error.restype = C.c_char_p
+    lib.refgpu_run.restype = C.c_int
+    lib.refgpu_run.argtypes = [C.c_char_p, _dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                               C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp]
+    assert U.dtype == np.float64 and U.flags.c_contiguous and U.shape == g.shape
+    assert all(b in ("transmissive", 0) for b in g.bc), "the reference GPU kernels are transmissive only"
+    ms = np.zeros(4)
+    dts = np.zeros(max(nsteps, 1))
+    s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+    rc = lib.refgpu_run(REFGPU_IMAGE.encode(), _p(U), g.nx, g.ny, g.x_min, g.x_max, g.y_min, g.y_max, s, cfl,
+                        int(warmup), int(nsteps), _p(ms), _p(dts))
+    if rc:
+        raise RuntimeError("reference GPU run failed: " + lib.refgpu_last_error().decode())
+    return dict(wall_ms=float(ms[0]), dt_ms=float(ms[1]), x_ms=float(ms[2]), y_ms=float(ms[3]), dts=dts[:nsteps])
+SFD_SO = os.path.join(HERE, "_build", "libshadowfd_euler2d.so")
+
+
+def frozen_fd(U0: np.ndarray, g: "Grid", dts, solver, dirs, eps: float, mask: np.ndarray, threads: int = 0):
+    """Branch-frozen central differences of J = sum(rho^2 over mask) after
+    len(dts) frozen-dt steps of the restatement (oracle/shadow_fd.cpp): the
+    runs from U0 +- eps d take the unperturbed run's branch decisions.
+    dirs: sequence of (rho, p) direction fields of shape (2, ny, nx).
+    Returns dict(J0, Jp, Jm, fd, flips, U) with one entry per direction in
+    fd / flips (decisions on which the +eps and -eps runs would differ) and
+    U the unperturbed run's final grid."""
+    lib = C.CDLL(SFD_SO)
+    lib.sfd_max_dirs.restype = C.c_int
+    lib.sfd_frozen_fd.restype = C.c_int
+    lib.sfd_frozen_fd.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                  C.POINTER(C.c_int), _dp, C.c_longlong, C.c_int, _dp, C.c_int, C.c_double,
+                                  C.POINTER(C.c_ubyte), _dp, C.POINTER(C.c_ulonglong), _dp]
+    nd = len(dirs)
+    assert 1 <= nd <= lib.sfd_max_dirs()
+    assert U0.dtype == np.float64 and U0.flags.c_contiguous and U0.shape == g.shape
+    D = np.ascontiguousarray(np.stack([np.asarray(d, dtype=np.float64).reshape(2, g.ny, g.nx) for d in dirs]))
+    M = np.ascontiguousarray(mask.reshape(g.ny, g.nx).astype(np.uint8))
+    dts = np.ascontiguousarray(np.asarray(dts, dtype=np.float64))
+    J = np.zeros(1 + 2 * nd)
+    flips = (C.c_ulonglong * nd)()
+    bc = (C.c_int * 4)(*[BC[b] if isinstance(b, str) else int(b) for b in g.bc])
+    s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+    if threads:
+        lib.sfd_set_threads_(C.c_int(threads))
+    UN = g.zeros()
+    rc = lib.sfd_frozen_fd(_p(U0), g.nx, g.ny, g.x_min, g.x_max, g.y_min, g.y_max, bc, _p(dts), len(dts), s,
+                           _p(D), nd, eps, M.ctypes.data_as(C.POINTER(C.c_ubyte)), _p(J), flips, _p(UN))
+    if rc:
+        raise RuntimeError(f"sfd_frozen_fd failed ({rc})")
+    Jp, Jm = J[1::2].copy(), J[2::2].copy()
+    return dict(J0=float(J[0]), Jp=Jp, Jm=Jm, fd=(Jp - Jm) / (2.0 * eps), flips=np.array(list(flips)), U=UN)
 
 
 def op_counts(U: np.ndarray, g: "Grid", cfl: float, t_end: float, solver="hllc", max_steps: int = 0) -> dict:
@@ -149,6 +225,8 @@ class Oracle:
             L.orc_compute_dt.restype = C.c_int
             L.orc_advance_second_order.argtypes = [_dp, _dp, _dp, G, C.c_double, C.c_int, _dp, _dp]
             L.orc_advance_first_order.argtypes = [_dp, _dp, G, C.c_double, C.c_int]
+            L.orc_sweep_x.argtypes = [_dp, _dp, G, C.c_double, C.c_int, _dp]
+            L.orc_sweep_y.argtypes = [_dp, _dp, G, C.c_double, C.c_int, _dp]
             L.orc_riemann_flux.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp]
             L.orc_run.argtypes = [_dp, G, C.c_double, C.c_double, C.c_int, C.c_longlong, C.c_int,
                                   _dp, _llp, _dp, C.c_longlong, _llp, _dp, _dp]
@@ -231,6 +309,18 @@ class Oracle:
             self._check_ref_grid(g)
             self.lib.ref_advance_second_order(_p(Uold), _p(Utmp), _p(Unew), *g.ext(), dt, s)
         return Utmp, Unew
+
+    def sweep_x(self, Uold, Utmp, g: Grid, dt: float, solver="hll"):
+        """x half of the split step (interior of Utmp from Uold), no ghost fill."""
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        gc = g.c()
+        self.lib.orc_sweep_x(_p(Uold), _p(Utmp), C.byref(gc), dt, s, None)
+
+    def sweep_y(self, Utmp, Unew, g: Grid, dt: float, solver="hll"):
+        """y half of the split step (interior of Unew from Utmp incl. its ghost rows), no ghost fill."""
+        s = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        gc = g.c()
+        self.lib.orc_sweep_y(_p(Utmp), _p(Unew), C.byref(gc), dt, s, None)
 
     def advance_first_order(self, Uold, g: Grid, dt: float, solver="hll"):
         s = SOLVERS[solver] if isinstance(solver, str) else int(solver)

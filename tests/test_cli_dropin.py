@@ -100,3 +100,42 @@ def test_cli_snapshots_match_oracle(cli, port, tmp_path, solver):
         Sref = ref["snapshots"][k - 1][j, i]
         for q in range(4):
             np.testing.assert_allclose(a[:, 4 + q], Sref[:, q], rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_shim_runs_the_reference_loop_on_the_gpu(cli, tmp_path, port):
+    """The shim under the reference's calling pattern, on the GPU: the loop of
+    scripts/cpu/main_cpu.cpp:217-262 (tests/dropin/run_shim.cpp, compiled
+    here against a stand-in of the reference's headers, since the reference
+    tree is not on the GPU host) runs the 256^2 blast to t_end with HLLC,
+    then with the exact solver in the same process (one device handle per
+    geometry, its solver switched per call).  Step counts equal the oracle's
+    and L1(rho) <= 1e-10 at t_end; an uninitialised workspace throws."""
+    exe = tmp_path / "run_shim"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "tests", "dropin"),
+                        "-I" + os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "dropin", "run_shim.cpp"),
+                        os.path.join(PKG, "shim", "solver_cpu_gb300.cpp"), "-L" + PKG, "-leuler2d",
+                        "-Wl,-rpath," + PKG, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    g = Grid(256, 256, 0.0, 2.0, 0.0, 2.0)
+    U0 = port.init_blast(g)
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        f.write(np.array([g.nx, g.ny], dtype=np.int32).tobytes())
+        f.write(np.array([g.x_min, g.x_max, g.y_min, g.y_max, 0.8, 0.25]).tobytes())
+        f.write(U0.tobytes())
+    solvers = ("hllc", "exact")
+    r = subprocess.run([str(exe), str(fin), str(fout), *solvers], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = open(fout, "rb").read()
+    rec = 16 + U0.nbytes
+    for k, solver in enumerate(solvers):
+        steps = int(np.frombuffer(raw[k * rec:k * rec + 8], dtype=np.int64)[0])
+        t = float(np.frombuffer(raw[k * rec + 8:k * rec + 16], dtype=np.float64)[0])
+        got = np.frombuffer(raw[k * rec + 16:(k + 1) * rec], dtype=np.float64).reshape(U0.shape)
+        V = U0.copy()
+        ref = port.run(V, g, 0.8, 0.25, solver)
+        assert steps == ref["steps"], (solver, steps, ref["steps"])
+        assert abs(t - ref["t"]) <= 1e-14
+        l1 = float(np.mean(np.abs(got[2:-2, 2:-2, 0] - V[2:-2, 2:-2, 0])))
+        assert l1 <= 1e-10, (solver, l1)

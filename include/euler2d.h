@@ -226,6 +226,33 @@ int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]);
  * rule dJ/dtheta = <dJ/dU_0, dU_0/dtheta> (large_sys_eq_opt_gb300/adjoint.py). */
 int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k);
 int eu_batch_adjoint_backward(eu_batch* b, const double* const* dJ_dUN, double* const* dJ_dU0);
+/* Scalar case parameters of one instance (no reference counterpart; the
+ * values of src/test_cases.cpp:24-101 made parameters):
+ *   kind 0, blast:        v = {cx, cy, R, rho_in, p_in, rho_out, p_out}
+ *   kind 1, shock-bubble: v = {rho0, p0, Mach, shock_x, bub_cx, bub_cy, bub_r,
+ *                              rho_bubble} */
+typedef struct {
+    int kind;
+    double v[8];
+} eu_case_params;
+/* The differentiable initial state of those parameters on the handle's grid,
+ * evaluated on the device at the cell centres: the blast with its interface
+ * as the one-cell linear ramp frac = clip(1/2 - (r - R)/h, 0, 1), h =
+ * min(dx, dy) (the cell average of a straight interface, so that the state
+ * is differentiable in R), the shock-bubble as src/test_cases.cpp:24-69. */
+int eu_init_params(eu_handle* h, const eu_case_params* p);
+/* Objective values and gradients with respect to two scalar parameters per
+ * instance, entirely on the device: each instance starts from
+ * eu_init_params(params[i]), runs nsteps[i] steps with the frozen step
+ * sizes dts[i] (checkpoints every ckpt_k), J_i = sum of rho^2 over the ring
+ * 0.6 <= r <= 0.8 from the blast centre or 1.2 r_b <= d <= 1.6 r_b from the
+ * bubble centre, and dJ_i/dtheta = <dJ/dU_0, dU_0/dtheta> with the closed-form
+ * tangents of the initial state.  dJ[2i], dJ[2i+1] = dJ/dR, dJ/dp_in (blast)
+ * or dJ/drho_bubble, dJ/dMach (shock-bubble).  Only these 3n numbers cross
+ * the host link.  Instances run concurrently on their streams, enqueued by
+ * several host threads. */
+int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const long long* nsteps,
+                             const double* const* dts, int ckpt_k, double* J, double* dJ);
 /* Test hook of the failure-detection path (no reference counterpart): with
  * n > 0 every y-sweep task waits for n more x-sweep tasks than exist, its
  * bounded wait (2 s) expires, and eu_batch_step returns EU_ERR_TIMEOUT with
@@ -289,6 +316,31 @@ int eu_write_planes(eu_handle* h, int which, const void* in, size_t bytes);
  * of the same grid. */
 int eu_save_state(eu_handle* h, const char* path);
 int eu_load_state(eu_handle* h, const char* path);
+/* ---- slab decomposition of one grid ------------------------------------------ */
+/* One grid split into nslabs slabs of whole rows, each with a 2-row halo:
+ * the semantics of the reference's domain decomposition
+ * (src/cpu/solver_mpi.cpp:246-291 partition, :340-402 and :547-573 halo
+ * exchange, :416-443 dt reduction) for slabs on the current device.  Per
+ * step: every slab's x-sweep, then the x-sweep outputs' two boundary rows
+ * copied into each neighbour's halo rows, every slab's y-sweep, then one dt
+ * for all slabs (the smallest of the slabs' proposals, which equals the
+ * undivided grid's CFL dt).  The results equal one handle's on the whole
+ * grid bit for bit.  Slab s holds interior rows [row0[s], row0[s+1]) with
+ * row0[s] = s*ny/nslabs; bc as eu_create (the outer sides only).  Needs
+ * ny >= 2*nslabs. */
+typedef struct eu_domain eu_domain;
+int eu_domain_plan(int ny, int nslabs, int* row0 /* nslabs + 1 */);
+int eu_domain_create(const eu_case* cfg, eu_precision prec, eu_solver solver, eu_limiter limiter, const int* bc,
+                     int nslabs, eu_domain** out);
+void eu_domain_destroy(eu_domain* d);
+const char* eu_domain_last_error(const eu_domain* d);
+/* The whole grid in the Grid2D AoS layout (ghosts included). */
+int eu_domain_upload_aos(eu_domain* d, const double* aos);
+int eu_domain_download_aos(eu_domain* d, double* aos);
+/* n CFL steps (clipped to t_end, which may be +inf), as eu_step_n. */
+int eu_domain_step_n(eu_domain* d, long long n, double t_end);
+int eu_domain_get_time(eu_domain* d, double* t, long long* steps);
+
 /* Device used by handles created afterwards on the calling thread. */
 int eu_set_device(int device);
 /* Name of device 0 and its SM count, for logs. */

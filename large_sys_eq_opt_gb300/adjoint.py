@@ -128,17 +128,37 @@ def objective_grad(U: np.ndarray, mask: np.ndarray) -> np.ndarray:
     return g
 
 
+PARAM_NAMES = {"blast": ("r", "p_in"), "shock_bubble": ("rho_bubble", "mach")}
+
+
 def ensemble_parameter_gradients(E, problems, nsteps: int, precision="fp32", solver="hllc", ckpt_k: int = 32,
-                                 batch=None):
+                                 batch=None, device=True):
     """J and dJ/dtheta of every instance after (at most) nsteps CFL steps.
 
     The dt sequences come from one ensemble run of the initial states (each
     instance stops at its own t_end); the adjoint forward and backward of all
-    instances then run concurrently.  Returns (J list, gradient dict list,
-    dts list, batch)."""
+    instances then run concurrently.  device=True keeps everything on the
+    GPU (initial states, objective, dJ/dU_N and the tangent contractions;
+    eu_batch_param_gradients); device=False is the same computation with
+    the grids passing through host arrays and the formulas of this module.
+    Returns (J list, gradient dict list, dts list, batch)."""
     own = batch is None
     b = batch if batch is not None else E.Batch(problems, precision, solver)
     try:
+        if device:
+            for inst, p in zip(b.instances, problems):
+                inst.init_params(p)
+                inst.set_dt_log(nsteps)
+            b.start()
+            b.step(nsteps)
+            dts = []
+            for inst in b.instances:
+                _, n, _ = inst.time()
+                dts.append(inst.dt_log(min(n, nsteps)))
+            J, dJ = b.param_gradients(problems, dts, ckpt_k)
+            kinds = ["blast" if isinstance(p.params, BlastParams) else "shock_bubble" for p in problems]
+            grads = [dict(zip(PARAM_NAMES[k], map(float, g))) for k, g in zip(kinds, dJ)]
+            return [float(x) for x in J], grads, dts, b
         states = [initial_state(p) for p in problems]
         for inst, (U0, _) in zip(b.instances, states):
             inst.upload(U0)

@@ -52,7 +52,8 @@ def units():
             out.append((os.path.join(CSRC, "adjoint_kernels.cu"), f"adj_{prec}_{solver}.o", flags))
     out.append((os.path.join(CSRC, "aux_kernels.cu"), "aux_kernels.o", []))
     out.append((os.path.join(CSRC, "noalloc.cu"), "noalloc.o", []))
-    for unit in ("runtime", "api", "api_adjoint", "api_batch"):
+    out.append((os.path.join(CSRC, "grad_kernels.cu"), "grad_kernels.o", []))
+    for unit in ("runtime", "api", "api_adjoint", "api_batch", "api_domain"):
         out.append((os.path.join(CSRC, unit + ".cpp"), unit + ".o", ["-x", "cu"]))
     return out
 

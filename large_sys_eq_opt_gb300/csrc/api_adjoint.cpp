@@ -222,15 +222,11 @@ int adj_fwd_finish(eu_handle* h) {
     return EU_OK;
 }
 
-int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
-    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
-    if (!dJ_dUN || !dJ_dU0) return fail(h, EU_ERR_INVALID, "eu_adjoint_backward: null argument");
+// The backward sweeps on the handle's stream: A.lam holds dJ/dU_N on entry
+// and dJ/dU_0 on exit (planes of a state buffer), each earlier segment's
+// states recomputed from its checkpoint.
+int adj_bwd_sweeps(eu_handle* h) {
     auto& A = h->adj;
-    if (!A.ready) return fail(h, EU_ERR_STATE, "eu_adjoint_backward: call eu_adjoint_forward first");
-    if (int rc = ensure_aos(h)) return rc;
-    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, dJ_dUN, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
-    if (h->prec == EU_FP32) EU_CUDA(h, launch_pack_aos<float>(h->d_aos, Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
-    else EU_CUDA(h, launch_pack_aos<double>(h->d_aos, Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
     EU_CUDA(h, cudaEventRecord(A.ev[2], h->st));
     for (int s = A.nseg - 1; s >= 0; --s) {
         if (A.ring_seg != s) {
@@ -241,6 +237,19 @@ int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
         for (int j = len - 1; j >= 0; --j) EU_CUDA(h, adj_step(h, s, j));
     }
     EU_CUDA(h, cudaEventRecord(A.ev[3], h->st));
+    return EU_OK;
+}
+
+int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {
+    if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
+    if (!dJ_dUN || !dJ_dU0) return fail(h, EU_ERR_INVALID, "eu_adjoint_backward: null argument");
+    auto& A = h->adj;
+    if (!A.ready) return fail(h, EU_ERR_STATE, "eu_adjoint_backward: call eu_adjoint_forward first");
+    if (int rc = ensure_aos(h)) return rc;
+    EU_CUDA(h, cudaMemcpyAsync(h->d_aos, dJ_dUN, aos_bytes(h), cudaMemcpyHostToDevice, h->st));
+    if (h->prec == EU_FP32) EU_CUDA(h, launch_pack_aos<float>(h->d_aos, Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
+    else EU_CUDA(h, launch_pack_aos<double>(h->d_aos, Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, h->cfg.nx, h->cfg.ny, h->st));
+    if (int rc = adj_bwd_sweeps(h)) return rc;
     const int bcz[4] = {0, 0, 0, 0};
     if (h->prec == EU_FP32) EU_CUDA(h, launch_unpack_aos<float>(Planes<float>{static_cast<float*>(A.lam), h->pitch_s, h->plane_s}, kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));
     else EU_CUDA(h, launch_unpack_aos<double>(Planes<double>{static_cast<double*>(A.lam), h->pitch_s, h->plane_s}, kSOff, h->cfg.nx, h->cfg.ny, bcz, h->d_aos, h->st));

@@ -335,3 +335,148 @@ int eu_batch_set_wait_extra(eu_batch* b, int n) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched gradients with respect to scalar case parameters, device-resident
+// ---------------------------------------------------------------------------
+#include <atomic>
+#include <thread>
+
+#include "grad_kernels.h"
+
+namespace {
+
+// Host-side derived values of one instance's parameters (see ParamState).
+ParamState param_state(const eu_handle* h, const eu_case_params& p) {
+    ParamState d{};
+    d.kind = p.kind;
+    for (int k = 0; k < 8; ++k) d.v[k] = p.v[k];
+    d.h = std::min(h->dx, h->dy);
+    if (p.kind == 1) {   // Rankine-Hugoniot post-shock state and its Mach derivatives (src/test_cases.cpp:35-46)
+        const double g = kGammaD, rho0 = p.v[0], p0 = p.v[1], M = p.v[2], M2 = M * M;
+        const double a0 = std::sqrt(g * p0 / rho0);
+        const double den = (g - 1.0) * M2 + 2.0;
+        d.ps[0] = rho0 * (g + 1.0) * M2 / den;
+        d.ps[1] = 2.0 * a0 / (g + 1.0) * (M - 1.0 / M);
+        d.ps[2] = p0 * (1.0 + 2.0 * g / (g + 1.0) * (M2 - 1.0));
+        d.ps[3] = rho0 * (g + 1.0) * 4.0 * M / (den * den);
+        d.ps[4] = 2.0 * a0 / (g + 1.0) * (1.0 + 1.0 / M2);
+        d.ps[5] = p0 * 2.0 * g / (g + 1.0) * 2.0 * M;
+    }
+    return d;
+}
+
+template <class T> cudaError_t init_params_t(eu_handle* h, const ParamState& d) {
+    return launch_init_param<T>(planes_s<T>(h, h->cur), h->cfg.nx, h->cfg.ny, h->cfg.x_min, h->cfg.y_min, h->dx,
+                                h->dy, d, h->st);
+}
+
+// Objective and dJ/dU_N into the adjoint buffer, the backward sweeps, and the
+// tangent contraction; results (J, dJ/dtheta_0, dJ/dtheta_1) at d_out.
+template <class T> int grad_tail_t(eu_handle* h, const ParamState& d, double* d_out) {
+    auto& A = h->adj;
+    const Planes<T> L{static_cast<T*>(A.lam), h->pitch_s, h->plane_s};
+    EU_CUDA(h, cudaMemsetAsync(A.lam, 0, state_bytes(h), h->st));
+    EU_CUDA(h, launch_objective<T>(planes_s<T>(h, h->cur), L, h->cfg.nx, h->cfg.ny, h->cfg.x_min, h->cfg.y_min,
+                                   h->dx, h->dy, d, h->d_part, h->part_blocks, d_out, h->st));
+    if (int rc = adj_bwd_sweeps(h)) return rc;
+    EU_CUDA(h, launch_tangent_dot<T>(L, h->cfg.nx, h->cfg.ny, h->cfg.x_min, h->cfg.y_min, h->dx, h->dy, d, h->d_part,
+                                     h->part_blocks, d_out + 1, h->st));
+    return EU_OK;
+}
+
+// Runs f(i) for i in [0, n) on up to `threads` host threads; the first
+// failing instance's code is returned.
+template <class F> int for_instances(int n, int threads, F f) {
+    std::atomic<int> next{0}, rc{EU_OK};
+    auto work = [&]() {
+        for (int i = next++; i < n; i = next++) {
+            const int r = f(i);
+            int ok = EU_OK;
+            if (r != EU_OK) rc.compare_exchange_strong(ok, r);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    return rc.load();
+}
+
+}  // namespace
+
+extern "C" {
+
+int eu_init_params(eu_handle* h, const eu_case_params* p) {
+    if (!h || !p || (p->kind != 0 && p->kind != 1)) return fail(h, EU_ERR_INVALID, "eu_init_params: bad argument");
+    const ParamState d = param_state(h, *p);
+    EU_CUDA(h, h->prec == EU_FP32 ? init_params_t<float>(h, d) : init_params_t<double>(h, d));
+    ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
+    if (int rc = ctl_push(h)) return rc;
+    drop_graphs(h);
+    EU_CUDA(h, cudaStreamSynchronize(h->st));
+    return EU_OK;
+}
+
+int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const long long* nsteps,
+                             const double* const* dts, int ckpt_k, double* J, double* dJ) {
+    Range range_("eu_batch_param_gradients");
+    if (!b || !params || !nsteps || !dts || !J || !dJ) return bfail(b, EU_ERR_INVALID, "bad argument");
+    for (int i = 0; i < b->n; ++i)
+        if (params[i].kind != 0 && params[i].kind != 1) return bfail(b, EU_ERR_INVALID, "bad parameter kind");
+    if (cudaStreamSynchronize(b->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "batch stream failed");
+    double *d_res = nullptr, *h_res = nullptr;
+    if (cudaMalloc(&d_res, sizeof(double) * 3 * (size_t)b->n) != cudaSuccess ||
+        cudaMallocHost(&h_res, sizeof(double) * 3 * (size_t)b->n) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaFree(d_res);
+        return bfail(b, EU_ERR_NOMEM, "eu_batch_param_gradients: result buffers");
+    }
+    std::vector<ParamState> ps;
+    for (int i = 0; i < b->n; ++i) ps.push_back(param_state(b->h[(size_t)i], params[i]));
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int threads = (int)std::max(1u, std::min(8u, hw ? hw : 1u));
+    // 1. every instance's initial state and checkpointed forward, enqueued
+    int rc = for_instances(b->n, threads, [&](int i) {
+        eu_handle* h = b->h[(size_t)i];
+        ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
+        if (int r = ctl_push(h)) return r;
+        drop_graphs(h);
+        const cudaError_t e = h->prec == EU_FP32 ? init_params_t<float>(h, ps[(size_t)i]) : init_params_t<double>(h, ps[(size_t)i]);
+        if (e != cudaSuccess) return cuda_fail(h, e, "parameter initial state");
+        return adj_fwd_enqueue(h, nsteps[i], dts[i], ckpt_k);
+    });
+    // 2. as each forward completes: objective, backward sweeps, contraction
+    if (rc == EU_OK)
+        rc = for_instances(b->n, threads, [&](int i) {
+            eu_handle* h = b->h[(size_t)i];
+            if (int r = adj_fwd_finish(h)) return r;
+            const int r = h->prec == EU_FP32 ? grad_tail_t<float>(h, ps[(size_t)i], d_res + 3 * i)
+                                             : grad_tail_t<double>(h, ps[(size_t)i], d_res + 3 * i);
+            if (r) return r;
+            EU_CUDA(h, cudaMemcpyAsync(h_res + 3 * i, d_res + 3 * i, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                       h->st));
+            return (int)EU_OK;
+        });
+    for (int i = 0; i < b->n; ++i) {
+        eu_handle* h = b->h[(size_t)i];
+        if (cudaStreamSynchronize(h->st) != cudaSuccess && rc == EU_OK) rc = cuda_fail(h, cudaGetLastError(), "sync");
+        if (rc == EU_OK) cudaEventElapsedTime(&h->adj.ms_bwd, h->adj.ev[2], h->adj.ev[3]);
+    }
+    if (rc == EU_OK)
+        for (int i = 0; i < b->n; ++i) {
+            J[i] = h_res[3 * i];
+            dJ[2 * i] = h_res[3 * i + 1];
+            dJ[2 * i + 1] = h_res[3 * i + 2];
+        }
+    cudaFree(d_res);
+    cudaFreeHost(h_res);
+    if (rc != EU_OK) {
+        for (int i = 0; i < b->n; ++i)
+            if (!b->h[(size_t)i]->err.empty()) return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+        return bfail(b, rc, "eu_batch_param_gradients failed");
+    }
+    return EU_OK;
+}
+
+}  // extern "C"

@@ -236,9 +236,37 @@ __global__ void totals_final_kernel(const double* part, int nblocks, double* out
     }
 }
 
+// One thread: the smallest proposed dt of n slabs to every slab (see
+// launch_domain_dt), with their status and stop flags merged.
+__global__ void domain_dt_kernel(Ctl* const* ctls, int n) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double dt = ctls[0]->dt, smax = ctls[0]->smax;
+    int status = 0, done = 0;
+    for (int s = 0; s < n; ++s) {
+        const Ctl* c = ctls[s];
+        if (c->dt < dt) dt = c->dt;
+        if (c->smax > smax) smax = c->smax;
+        status |= c->status;
+        done |= c->done;
+    }
+    for (int s = 0; s < n; ++s) {
+        Ctl* c = ctls[s];
+        c->dt = dt;
+        c->smax = smax;
+        c->status = status;
+        c->done = done;
+    }
+    __threadfence();
+}
+
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
+cudaError_t launch_domain_dt(Ctl* const* ctls, int n, cudaStream_t s) {
+    domain_dt_kernel<<<1, 32, 0, s>>>(ctls, n);
+    return cudaGetLastError();
+}
+
 static int grid_for(long long n, int threads) {
     long long b = (n + threads - 1) / threads;
     const long long cap = 16LL * sm_count_current();   // grid-stride loops: 16 CTAs per SM at most

@@ -30,6 +30,13 @@ template <class T>
 cudaError_t launch_totals(Planes<T> P, int coff, int nx, int ny, double* part, int max_blocks, double* out,
                           cudaStream_t s);
 
+// Slab decomposition: the step size common to n sub-domains.  Every slab's
+// step finalisation has proposed dt = cfl min(dx, dy) / (its own maximum
+// signal speed), clipped to t_end; the grid's dt is the smallest proposal
+// (x -> c / x is monotone and correctly rounded, so this equals the dt of
+// the undivided grid bit for bit), and a status or stop of any slab stops all.
+cudaError_t launch_domain_dt(Ctl* const* ctls, int n, cudaStream_t s);
+
 // One entry per (precision, solver) translation unit of kern_sweeps.cu.
 SweepKernels sweep_kernels_32_0();
 SweepKernels sweep_kernels_32_1();

@@ -222,6 +222,7 @@ void adj_free(eu_handle* h);
 int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k);
 int adj_fwd_finish(eu_handle* h);
 int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0);
+int adj_bwd_sweeps(eu_handle* h);
 int adj_bwd_finish(eu_handle* h, double* dJ_dU0);
 
 // Ensembles (api_batch.cpp).

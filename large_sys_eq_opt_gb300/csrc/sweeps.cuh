@@ -80,8 +80,16 @@ template <class T, int S> struct Line {
     // and the caller redoes the work with SLOW = true when one matters.
     template <bool SLOW>
     __device__ __forceinline__ Cons<T> step(const Cons<T>& U, T hl, T lam, bool& fi, bool& fc, bool& ff) {
-        bool isl = false, slow_cell = false, slow_face = !rp_phys;
-        Prim<T> W = c2p_fast(U, isl);
+        bool isl = false;
+        const Prim<T> W = c2p_fast(U, isl);
+        return step_w<SLOW>(U, W, isl, hl, lam, fi, fc, ff);
+    }
+    // step() with the cell's c2p_fast primitives W and island flag isl given
+    // (computed ahead, two cells at a time).
+    template <bool SLOW>
+    __device__ __forceinline__ Cons<T> step_w(const Cons<T>& U, Prim<T> W, bool isl, T hl, T lam, bool& fi,
+                                              bool& fc, bool& ff) {
+        bool slow_cell = false, slow_face = !rp_phys;
         const bool nice = nice_cell(W);
         Face<T> L, R;
         Prim<T> dp;
@@ -118,6 +126,28 @@ template <class T, int S> struct Line {
     __device__ __forceinline__ Cons<T> push(const Cons<T>& U, T hl, T lam) {
         bool a = false, b = false, c = false;
         return step<true>(U, hl, lam, a, b, c);
+    }
+    // The fast path only, with the cell's primitives W given (c2p_fast of U,
+    // computed ahead for two rows at a time) and one flag for every
+    // fallback the push could need (the cell's FP64 pressure island included
+    // by the caller); the y-sweep's fast pass.
+    __device__ __forceinline__ Cons<T> step_fast(const Cons<T>& U, const Prim<T>& W, T hl, T lam, bool& flag) {
+        const bool nice = nice_cell(W);
+        Face<T> L, R;
+        Prim<T> dp;
+        bool slow = !rp_phys;
+        reconstruct_fast(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow, dp);
+        const Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);
+        flag |= slow;
+        const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
+        A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
+        dm = dp;
+        Wm1 = W;
+        Um1 = U;
+        Rp = R;
+        nice2 = nice1; nice1 = nice;
+        rp_phys = true;
+        return N;
     }
 };
 
@@ -365,10 +395,29 @@ __device__ __forceinline__ bool x_task(const CUtensorMap* tm, const CUtensorMap*
             ld_vec<T, HV>(q + 32 * CX, mn);
             ld_vec<T, HV>(q + 64 * CX, mt);
             ld_vec<T, HV>(q + 96 * CX, en);
+            if constexpr (sizeof(T) == 4) {
+                // FP32: the cells' primitives two at a time (packed), then the pushes
+                Prim<T> W[HV];
+                bool isl[HV];
 #pragma unroll
-            for (int v = 0; v < HV; ++v) {
-                const Cons<T> N = line.push(Cons<T>{r[v], mn[v], mt[v], en[v]}, hl, lam);
-                r[v] = N.r; mn[v] = N.mn; mt[v] = N.mt; en[v] = N.e;
+                for (int v = 0; v < HV; v += 2) {
+                    isl[v] = isl[v + 1] = false;
+                    c2p_rows(Cons<T>{r[v], mn[v], mt[v], en[v]}, Cons<T>{r[v + 1], mn[v + 1], mt[v + 1], en[v + 1]},
+                             W[v], W[v + 1], isl[v], isl[v + 1]);
+                }
+#pragma unroll
+                for (int v = 0; v < HV; ++v) {
+                    bool a = false, b = false, c = false;
+                    const Cons<T> N = line.template step_w<true>(Cons<T>{r[v], mn[v], mt[v], en[v]}, W[v], isl[v],
+                                                                 hl, lam, a, b, c);
+                    r[v] = N.r; mn[v] = N.mn; mt[v] = N.mt; en[v] = N.e;
+                }
+            } else {
+#pragma unroll
+                for (int v = 0; v < HV; ++v) {
+                    const Cons<T> N = line.push(Cons<T>{r[v], mn[v], mt[v], en[v]}, hl, lam);
+                    r[v] = N.r; mn[v] = N.mn; mt[v] = N.mt; en[v] = N.e;
+                }
             }
             st_vec<T, HV>(q, r);                  // outputs overwrite their inputs in place
             st_vec<T, HV>(q + 32 * CX, mn);
@@ -564,19 +613,41 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
         if (k == 0) {   // window of the line's first cell (see Line::prime)
             line.prime(Cons<T>{sb[0], sb[2 * RY * BW], sb[RY * BW], sb[3 * RY * BW]});
         }
+        // FP32 fast pass: the box's cells are converted to primitives two
+        // rows at a time (packed), and the outputs' signal speeds likewise
+        constexpr bool kRows = FAST && sizeof(T) == 4;
+        Cons<T> Ub[RY];
+        Prim<T> Wb[RY];
+        bool ib[RY];
+        if constexpr (kRows) {
+#pragma unroll
+            for (int rr = 0; rr < RY; ++rr) {
+                Ub[rr] = Cons<T>{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
+                ib[rr] = false;
+            }
+#pragma unroll
+            for (int rr = 0; rr < RY; rr += 2) c2p_rows(Ub[rr], Ub[rr + 1], Wb[rr], Wb[rr + 1], ib[rr], ib[rr + 1]);
+        }
+        Cons<T> Nprev{};
 #pragma unroll
         for (int rr = 0; rr < RY; ++rr) {
             // normal momentum of the y-sweep is rho*v (plane 2)
-            const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
             Cons<T> N;
-            if constexpr (FAST) {
+            if constexpr (kRows) {
                 // a flag matters unless the push lies past the task's last
                 // output row (no later output depends on it)
-                bool fi = false, fc = false, ff = false;
-                N = line.template step<false>(U, hl, lam, fi, fc, ff);
-                flag |= (fi | fc | ff) & (((live_mask >> rr) & 1u) != 0u);
+                bool f = ib[rr];
+                N = line.step_fast(Ub[rr], Wb[rr], hl, lam, f);
+                flag |= f & (((live_mask >> rr) & 1u) != 0u);
             } else {
-                N = line.push(U, hl, lam);
+                const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
+                if constexpr (FAST) {
+                    bool fi = false, fc = false, ff = false;
+                    N = line.template step<false>(U, hl, lam, fi, fc, ff);
+                    flag |= (fi | fc | ff) & (((live_mask >> rr) & 1u) != 0u);
+                } else {
+                    N = line.push(U, hl, lam);
+                }
             }
             ob[rr * 32] = N.r;
             ob[(RY + rr) * 32] = N.mt;
@@ -584,13 +655,26 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
             ob[(3 * RY + rr) * 32] = N.e;
             const int ir = ir0 + rr;
             const bool out_ok = ((out_mask >> rr) & 1u) != 0u;
-            const T sp = signal_speed_fast(N);
-            if (out_ok) {
-                if constexpr (sizeof(T) == 4) {
-                    smax = max_nan(smax, sp);     // NaN propagates: checked once at the end
+            if constexpr (kRows) {
+                if (rr & 1) {             // the speeds of rows rr-1 and rr
+                    // selects, not branches: a speed is >= 0 or NaN, so 0
+                    // stands in for a row without an output
+                    const float2 sp = signal_speed_rows(Nprev, N);
+                    const float s0 = ((out_mask >> (rr - 1)) & 1u) ? sp.x : 0.0f;
+                    const float s1 = out_ok ? sp.y : 0.0f;
+                    smax = max_nan(smax, max_nan(s0, s1));
                 } else {
-                    ssum += sp;                   // NaN / inf propagate: checked once at the end
-                    smax = Ar<T>::fmax_(smax, sp);
+                    Nprev = N;
+                }
+            } else {
+                const T sp = signal_speed_fast(N);
+                if (out_ok) {
+                    if constexpr (sizeof(T) == 4) {
+                        smax = max_nan(smax, sp);     // NaN propagates: checked once at the end
+                    } else {
+                        ssum += sp;                   // NaN / inf propagate: checked once at the end
+                        smax = Ar<T>::fmax_(smax, sp);
+                    }
                 }
             }
             if (special) {                        // warp-uniform: few warps store anything directly

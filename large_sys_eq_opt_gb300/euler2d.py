@@ -39,6 +39,21 @@ class EuCase(C.Structure):
                 ("cfl", C.c_double), ("t_end", C.c_double)]
 
 
+class EuCaseParams(C.Structure):
+    """eu_case_params: kind 0 blast (cx, cy, R, rho_in, p_in, rho_out, p_out),
+    kind 1 shock-bubble (rho0, p0, mach, shock_x, bub_cx, bub_cy, bub_r, rho_bubble)."""
+    _fields_ = [("kind", C.c_int), ("v", C.c_double * 8)]
+
+
+def case_params(prob: Problem) -> EuCaseParams:
+    from .cases import BlastParams
+    q = prob.params
+    if isinstance(q, BlastParams):
+        return EuCaseParams(0, (C.c_double * 8)(q.cx, q.cy, q.r, q.rho_in, q.p_in, q.rho_out, q.p_out, 0.0))
+    return EuCaseParams(1, (C.c_double * 8)(q.rho0, q.p0, q.mach, q.shock_x, q.bub_cx, q.bub_cy, q.bub_r,
+                                            q.rho_bubble))
+
+
 class EuRunInfo(C.Structure):
     _fields_ = [("t", C.c_double), ("steps", C.c_longlong), ("status", C.c_int), ("nsnap_written", C.c_int)]
 
@@ -58,7 +73,9 @@ EXPORTS = (
     "eu_batch_create", "eu_batch_destroy", "eu_batch_last_error", "eu_batch_handle", "eu_batch_start",
     "eu_batch_step", "eu_batch_run", "eu_batch_time_steps", "eu_batch_autotune",
     "eu_batch_adjoint_forward", "eu_batch_adjoint_backward", "eu_batch_set_wait_extra", "eu_write_planes",
-    "eu_save_state", "eu_load_state",
+    "eu_save_state", "eu_load_state", "eu_domain_plan", "eu_domain_create", "eu_domain_destroy",
+    "eu_domain_last_error", "eu_domain_upload_aos", "eu_domain_download_aos", "eu_domain_step_n",
+    "eu_domain_get_time", "eu_init_params", "eu_batch_param_gradients",
 )
 
 _lib = None
@@ -141,8 +158,87 @@ def load(path: str = LIB_PATH):
     L.eu_write_planes.argtypes = [H, C.c_int, C.c_void_p, C.c_size_t]
     L.eu_save_state.argtypes = [H, C.c_char_p]
     L.eu_load_state.argtypes = [H, C.c_char_p]
+    L.eu_init_params.argtypes = [H, C.POINTER(EuCaseParams)]
+    L.eu_batch_param_gradients.argtypes = [B, C.POINTER(EuCaseParams), C.POINTER(C.c_longlong), C.POINTER(_dp),
+                                           C.c_int, _dp, _dp]
+    D = C.c_void_p
+    L.eu_domain_plan.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int)]
+    L.eu_domain_create.argtypes = [C.POINTER(EuCase), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int,
+                                   C.POINTER(D)]
+    L.eu_domain_destroy.argtypes = [D]
+    L.eu_domain_destroy.restype = None
+    L.eu_domain_last_error.argtypes = [D]
+    L.eu_domain_last_error.restype = C.c_char_p
+    L.eu_domain_upload_aos.argtypes = [D, _dp]
+    L.eu_domain_download_aos.argtypes = [D, _dp]
+    L.eu_domain_step_n.argtypes = [D, C.c_longlong, C.c_double]
+    L.eu_domain_get_time.argtypes = [D, _dp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
+
+
+def domain_plan(ny: int, nslabs: int):
+    """First interior row of each slab (and ny) of the slab decomposition."""
+    L = load()
+    out = (C.c_int * (nslabs + 1))()
+    rc = L.eu_domain_plan(int(ny), int(nslabs), out)
+    if rc:
+        raise EulerError(rc, L.eu_last_error(None).decode())
+    return [int(x) for x in out]
+
+
+class Domain:
+    """One grid split into slabs of whole rows on the current device, each a
+    handle with a 2-row halo exchanged every step (eu_domain_*); results equal
+    a single Solver's bit for bit."""
+
+    def __init__(self, cfg: CaseConfig, precision="fp64", solver="hllc", bc=(0, 0, 0, 0), nslabs=2):
+        self._L = L = load()
+        self.cfg = cfg
+        c = EuCase(cfg.nx, cfg.ny, cfg.ng, cfg.x_min, cfg.x_max, cfg.y_min, cfg.y_max, cfg.cfl, cfg.t_end)
+        b = (C.c_int * 4)(*bc)
+        d = C.c_void_p()
+        prec = FP32 if precision in ("fp32", FP32) else FP64
+        rc = L.eu_domain_create(C.byref(c), prec, SOLVERS[solver], 0, b, int(nslabs), C.byref(d))
+        if rc:
+            raise EulerError(rc, L.eu_domain_last_error(None).decode())
+        self._d = d
+
+    def _check(self, rc):
+        if rc:
+            raise EulerError(rc, self._L.eu_domain_last_error(self._d).decode())
+
+    def upload(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        self._check(self._L.eu_domain_upload_aos(self._d, _p(U)))
+
+    def download(self) -> np.ndarray:
+        U = np.zeros((self.cfg.ny + 4, self.cfg.nx + 4, 4))
+        self._check(self._L.eu_domain_download_aos(self._d, _p(U)))
+        return U
+
+    def step_n(self, n: int, t_end: float = float("inf")):
+        self._check(self._L.eu_domain_step_n(self._d, int(n), float(t_end)))
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_longlong()
+        self._check(self._L.eu_domain_get_time(self._d, C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def close(self):
+        if getattr(self, "_d", None):
+            self._L.eu_domain_destroy(self._d)
+            self._d = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def _p(a: np.ndarray):
@@ -420,6 +516,11 @@ class Solver:
     def load_state(self, path: str):
         self._check(self._L.eu_load_state(self._h, str(path).encode()))
 
+    def init_params(self, prob: Problem):
+        """The differentiable initial state of prob's parameters (eu_init_params)."""
+        p = case_params(prob)
+        self._check(self._L.eu_init_params(self._h, C.byref(p)))
+
     def autotune(self, steps: int = 20):
         """Measure and set the fastest segment lengths; returns (seg_x, seg_y)."""
         out = (C.c_longlong * 2)()
@@ -497,6 +598,20 @@ class Batch:
         ptrs = (_dp * n)(*[_p(a) for a in arrs])
         self._keep = arrs
         self._check(self._L.eu_batch_adjoint_forward(self._b, ns, ptrs, int(ckpt_k)))
+
+    def param_gradients(self, problems, dts_list, ckpt_k: int = 32):
+        """J and the gradients with respect to each instance's two scalar
+        parameters, all on the device (eu_batch_param_gradients).  Returns
+        (J array of n, dJ array of n x 2)."""
+        n = len(self.instances)
+        params = (EuCaseParams * n)(*[case_params(p) for p in problems])
+        dts = [np.ascontiguousarray(d, dtype=np.float64) for d in dts_list]
+        ns = (C.c_longlong * n)(*[len(d) for d in dts])
+        pd = (_dp * n)(*[_p(d) for d in dts])
+        J = np.zeros(n)
+        dJ = np.zeros(2 * n)
+        self._check(self._L.eu_batch_param_gradients(self._b, params, ns, pd, int(ckpt_k), _p(J), _p(dJ)))
+        return J, dJ.reshape(n, 2)
 
     def adjoint_backward(self, grads_N):
         """dJ/dU_0 of every instance from its dJ/dU_N (concurrently)."""

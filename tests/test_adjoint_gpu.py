@@ -283,15 +283,17 @@ def test_adjoint_config_512_branch_frozen_fd(E):
     """The adjoint benchmark size against branch-frozen central differences:
     512^2 perturbed blast, HLLC + minmod, 400 steps on the oracle's frozen
     dt sequence, checkpoints every 32, 16 portable seeded Gaussian
-    directions, eps = 1e-6.  The reference values come from the CPU oracle
-    run three ways at once (tests/golden/frozen_fd_512.json, made by
-    tests/golden/make_frozen_fd.py): the +-eps runs replay the unperturbed
-    run's limiter, fallback and Riemann branch decisions, so no kink is
-    crossed inside the difference and the quotient converges at O(eps^2).
-    The FP64 GPU adjoint must match every direction to 1e-6 relative.  The
-    fixture also counts, per direction, the decisions on which free +eps and
-    -eps runs would differ: those flips are what limits the unfrozen check
-    above."""
+    directions.  The reference values come from the CPU oracle run with
+    every lane's branch decisions taken from the unperturbed run
+    (tests/golden/frozen_fd_512.json, made by tests/golden/make_frozen_fd.py),
+    so no limiter or fallback kink is crossed inside the difference and the
+    quotient's truncation error is O(eps^2).  What limits a difference
+    quotient of 400 FP64 steps is then rounding noise in the +-eps runs,
+    which grows as 1/eps: at eps = 1e-3 the quotient is good to ~1e-8 and
+    the FP64 GPU adjoint must match every direction to 1e-6; at eps = 1e-6
+    (reported) the noise alone is ~1e-5.  The fixture also counts, per
+    direction, the decisions on which free +eps and -eps runs would differ:
+    those flips are what limits the unfrozen check above."""
     import json
     import sys
     gold = os.path.join(ROOT, "tests", "golden")
@@ -305,7 +307,8 @@ def test_adjoint_config_512_branch_frozen_fd(E):
     U0 = M.initial_grid(n, rho, p)
     dts = np.array(d["dts"])
     mask = M.ring(n)
-    dirs = M.directions(n, len(d["fd"]), d["seed"])
+    big, small = d["by_eps"]["0.001"], d["by_eps"]["1e-06"]
+    dirs = M.directions(n, len(big["fd"]), d["seed"])
     with E.Solver(geometry(n), "fp64", d["solver"]) as s:
         s.upload(U0)
         s.adjoint_forward(dts, 32)
@@ -314,10 +317,11 @@ def test_adjoint_config_512_branch_frozen_fd(E):
     J = objective(UN, mask)
     assert abs(J - d["J0"]) <= 1e-10 * abs(d["J0"]), (J, d["J0"])
     ad = adjoint_dirs(g, dirs)
-    fd = np.array(d["fd"])
-    rel = np.abs(ad - fd) / np.abs(fd)
-    print("branch-frozen fd rel errors", ["%.1e" % e for e in rel], "max %.2e" % rel.max())
-    print("branch flips between the +eps and -eps runs per direction", d["flips"])
+    rel = np.abs(ad - np.array(big["fd"])) / np.abs(np.array(big["fd"]))
+    rel6 = np.abs(ad - np.array(small["fd"])) / np.abs(np.array(small["fd"]))
+    print("branch-frozen fd, eps 1e-3: rel errors", ["%.1e" % e for e in rel], "max %.2e" % rel.max())
+    print("branch-frozen fd, eps 1e-6: rel errors", ["%.1e" % e for e in rel6], "median %.2e" % np.median(rel6))
+    print("branch flips between free +eps and -eps runs per direction (eps 1e-6)", small["flips"])
     assert rel.max() <= 1e-6
 
 

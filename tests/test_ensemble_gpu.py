@@ -113,3 +113,27 @@ def test_batched_parameter_gradients_match_fd(E):
                 fd = (J2[0] - J2[1]) / (2 * eps)
                 print(p.name or p.kind, name, "adjoint %.10e fd %.10e" % (val, fd))
                 assert abs(val - fd) <= 1e-5 * abs(fd) + 1e-9 * abs(J), (p, name, val, fd)
+
+
+def test_device_parameter_gradients_equal_host_path(E):
+    """eu_batch_param_gradients (initial states, objective, dJ/dU_N and the
+    tangent contractions on the device) against the same computation with
+    the grids passing through host arrays (adjoint.py formulas), FP64: the
+    same J and gradients to rounding."""
+    from large_sys_eq_opt_gb300 import adjoint as A
+    bub = (TRANSMISSIVE, TRANSMISSIVE, REFLECTIVE, REFLECTIVE)
+    probs = [
+        Problem(CaseConfig(64, 64, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.25), "blast", BlastParams(r=0.37, p_in=12.0)),
+        Problem(CaseConfig(140, 55, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.1), "shock_bubble",
+                ShockBubbleParams(mach=1.7, rho_bubble=0.4), bc=bub),
+    ]
+    Jd, gd, dtd, _ = A.ensemble_parameter_gradients(E, probs, 40, precision="fp64", solver="hllc", ckpt_k=8)
+    Jh, gh, dth, _ = A.ensemble_parameter_gradients(E, probs, 40, precision="fp64", solver="hllc", ckpt_k=8,
+                                                    device=False)
+    for a, b in zip(dtd, dth):
+        assert np.array_equal(a, b)
+    for a, b in zip(Jd, Jh):
+        assert abs(a - b) <= 1e-12 * abs(b)
+    for a, b in zip(gd, gh):
+        for k in b:
+            assert abs(a[k] - b[k]) <= 1e-9 * abs(b[k]) + 1e-12, (k, a[k], b[k])

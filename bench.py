@@ -422,10 +422,11 @@ def developed_leg(E, np, prob, dist, t_dev=0.2):
     return res
 
 
-def e2e_leg(E, prob, precision, solver, dist, ke=5):
+def e2e_leg(E, prob, precision, solver, dist, ke=10, warm=3):
     """The metric through the drop-in call on host grids: eu_step_host
     (Grid2D AoS in, BC + compute_dt + advance_second_order, Grid2D AoS out),
-    pinned host buffers, one warm-up step then `ke` timed steps."""
+    pinned host buffers, `warm` warm-up steps then `ke` timed steps (the
+    first calls of a process page in the pinned buffers and staging)."""
     n = prob.cfg.nx
     cells = prob.cfg.nx * prob.cfg.ny
     se = E.Solver.for_problem(prob, precision, solver)
@@ -433,7 +434,11 @@ def e2e_leg(E, prob, precision, solver, dist, ke=5):
     B = E.PinnedGrid(prob.cfg.nx, prob.cfg.ny)
     se.download(A.array)
     t, t_end = 0.0, 1e30
-    t += se.step_host(A.array, B.array, 0.8, t, t_end)   # warm-up
+    for k in range(warm):                                  # warm-up
+        src, dst = (A, B) if k % 2 == 0 else (B, A)
+        t += se.step_host(src.array, dst.array, 0.8, t, t_end)
+    if warm % 2 == 0:
+        A, B = B, A                                        # B holds the latest state
     dist.barrier()
     t0 = time.perf_counter()
     step_s = []

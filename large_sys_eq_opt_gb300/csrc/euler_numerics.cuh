@@ -835,8 +835,10 @@ __device__ __forceinline__ void face_state(const Prim<T>& W, Cons<T>& U, Cons<T>
 // marching line carries it from the previous cell, whose right difference
 // it is) and the right difference dp = W(c+1) - W(c) is returned.  `nice`
 // must say that all three cells pass nice_cell().
+// (reconstruct_fast_1: this form for every precision; reconstruct_fast: the
+// same, with the FP32 specialisation below that pairs the two faces.)
 template <class T>
-__device__ __forceinline__ void reconstruct_fast(const Prim<T>& dm, const Prim<T>& Wc, const Prim<T>& Wp, T hl,
+__device__ __forceinline__ void reconstruct_fast_1(const Prim<T>& dm, const Prim<T>& Wc, const Prim<T>& Wp, T hl,
                                                    bool nice, Face<T>& L, Face<T>& R, bool& slow, Prim<T>& dp) {
     dp = Prim<T>{Wp.r - Wc.r, Wp.un - Wc.un, Wp.ut - Wc.ut, Wp.p - Wc.p, T(0)};
     Prim<T> s;
@@ -855,6 +857,11 @@ __device__ __forceinline__ void reconstruct_fast(const Prim<T>& dm, const Prim<T
     L.V = c2p_fast(L.U, slow);
     R.V = c2p_fast(R.U, slow);
     slow |= !(nice && phys_recon_fast(L.V) && phys_recon_fast(R.V));
+}
+template <class T>
+__device__ __forceinline__ void reconstruct_fast(const Prim<T>& dm, const Prim<T>& Wc, const Prim<T>& Wp, T hl,
+                                                 bool nice, Face<T>& L, Face<T>& R, bool& slow, Prim<T>& dp) {
+    reconstruct_fast_1(dm, Wc, Wp, hl, nice, L, R, slow, dp);
 }
 
 // FP32: the same reconstruction with the left and right face states held as

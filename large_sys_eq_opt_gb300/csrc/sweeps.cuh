@@ -93,7 +93,8 @@ template <class T, int S> struct Line {
         const bool nice = nice_cell(W);
         Face<T> L, R;
         Prim<T> dp;
-        reconstruct_fast(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell, dp);
+        if constexpr (S == kExact) reconstruct_fast_1(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell, dp);
+        else reconstruct_fast(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow_cell, dp);
         Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow_face);
         bool r_phys = true;
         Prim<T> dnext = dp;   // W(c) - W(c-1) for the next cell
@@ -395,8 +396,9 @@ __device__ __forceinline__ bool x_task(const CUtensorMap* tm, const CUtensorMap*
             ld_vec<T, HV>(q + 32 * CX, mn);
             ld_vec<T, HV>(q + 64 * CX, mt);
             ld_vec<T, HV>(q + 96 * CX, en);
-            if constexpr (sizeof(T) == 4) {
-                // FP32: the cells' primitives two at a time (packed), then the pushes
+            if constexpr (sizeof(T) == 4 && S != kExact) {
+                // FP32: the cells' primitives two at a time (packed), then the
+                // pushes (not for the exact solver: it spilled)
                 Prim<T> W[HV];
                 bool isl[HV];
 #pragma unroll
@@ -615,7 +617,9 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
         }
         // FP32 fast pass: the box's cells are converted to primitives two
         // rows at a time (packed), and the outputs' signal speeds likewise
-        constexpr bool kRows = FAST && sizeof(T) == 4;
+        // (not for the exact solver, whose register-heavy Riemann call
+        // spilled with four rows' primitives held ahead)
+        constexpr bool kRows = FAST && sizeof(T) == 4 && S != kExact;
         Cons<T> Ub[RY];
         Prim<T> Wb[RY];
         bool ib[RY];

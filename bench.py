@@ -598,7 +598,11 @@ def run_ours(args, dist: Dist):
                        "frac": achieved / peak, "traffic": traffic, "kernel": dom,
                        "peak_source": f"{peak_kind} hbm_gbs",
                        "per_kernel_ms": {"sweep_x": tx / K, "sweep_y": ty / K},
-                       "algorithmic_bytes_per_launch": bytes_per_launch}
+                       "algorithmic_bytes_per_launch": bytes_per_launch,
+                       # the whole step: 64 B (FP32) per cell-update over the step time
+                       "step": {"achieved": 2 * bytes_per_launch / (tmax / K / 1e3) / 1e9,
+                                "frac": 2 * bytes_per_launch / (tmax / K / 1e3) / 1e9 / peak,
+                                "algorithmic_bytes_per_step": 2 * bytes_per_launch}}
     out["clocks"] = clk.summary()
     fl = reference_flops(args.solver)
     if fl is not None:
@@ -681,7 +685,8 @@ def run_ours(args, dist: Dist):
         summ = {"fp32_value": value, "fp32_e2e": out.get("e2e", {}).get("value"),
                 "fp64_value": out.get("fp64", {}).get("value"), "fp64_e2e": out.get("e2e_fp64", {}).get("value"),
                 "cpu_baseline_fp64": out.get("cpu_baseline", {}).get("value"),
-                "roofline_frac": out["roofline"]["frac"], "roofline_kernel": out["roofline"]["kernel"]}
+                "roofline_frac": out["roofline"]["frac"], "roofline_kernel": out["roofline"]["kernel"],
+                "roofline_frac_step": out["roofline"]["step"]["frac"]}
         cb = summ["cpu_baseline_fp64"]
         for k in ("fp32_value", "fp32_e2e", "fp64_value", "fp64_e2e"):
             if cb and summ[k]:

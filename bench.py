@@ -483,7 +483,9 @@ def ensemble_leg(E, np, steps=20):
         A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b)
         t_first = time.perf_counter() - t0
         t0 = time.perf_counter()
-        Js, grads, dts, _ = A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b)
+        parts = {}
+        Js, grads, dts, _ = A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b,
+                                                           timing=parts)
         t_all = time.perf_counter() - t0
         fwd_ms = max(inst.adjoint_timing()[0] for inst in b.instances)
         bwd_ms = max(inst.adjoint_timing()[1] for inst in b.instances)
@@ -501,6 +503,7 @@ def ensemble_leg(E, np, steps=20):
                    "tangent contractions on the device; 3 numbers per instance to the host)",
            "plain_ensemble_forward_ms": plain_ms, "gradients_wall_s_total": t_all,
            "gradients_wall_s_first_call": t_first, "gradients_over_plain_forward": t_all * 1e3 / plain_ms,
+           "wall_s_dt_run": parts.get("dt_run_s"), "wall_s_param_gradients_call": parts.get("gradients_s"),
            "checkpointed_forward_ms_max_instance": fwd_ms, "backward_device_ms_max_instance": bwd_ms,
            "example_gradients": grads[:2] + grads[48:50]}
     seq_ms = 0.0

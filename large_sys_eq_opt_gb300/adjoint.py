@@ -132,7 +132,7 @@ PARAM_NAMES = {"blast": ("r", "p_in"), "shock_bubble": ("rho_bubble", "mach")}
 
 
 def ensemble_parameter_gradients(E, problems, nsteps: int, precision="fp32", solver="hllc", ckpt_k: int = 32,
-                                 batch=None, device=True):
+                                 batch=None, device=True, timing: dict | None = None):
     """J and dJ/dtheta of every instance after (at most) nsteps CFL steps.
 
     The dt sequences come from one ensemble run of the initial states (each
@@ -141,11 +141,15 @@ def ensemble_parameter_gradients(E, problems, nsteps: int, precision="fp32", sol
     GPU (initial states, objective, dJ/dU_N and the tangent contractions;
     eu_batch_param_gradients); device=False is the same computation with
     the grids passing through host arrays and the formulas of this module.
-    Returns (J list, gradient dict list, dts list, batch)."""
+    Returns (J list, gradient dict list, dts list, batch); `timing`, when
+    given, receives the wall seconds of the dt run ("dt_run_s") and of the
+    gradient call ("gradients_s") on the device path."""
     own = batch is None
     b = batch if batch is not None else E.Batch(problems, precision, solver)
     try:
         if device:
+            import time
+            t0 = time.perf_counter()
             for inst, p in zip(b.instances, problems):
                 inst.init_params(p)
                 inst.set_dt_log(nsteps)
@@ -155,7 +159,11 @@ def ensemble_parameter_gradients(E, problems, nsteps: int, precision="fp32", sol
             for inst in b.instances:
                 _, n, _ = inst.time()
                 dts.append(inst.dt_log(min(n, nsteps)))
+            t1 = time.perf_counter()
             J, dJ = b.param_gradients(problems, dts, ckpt_k)
+            if timing is not None:
+                timing["dt_run_s"] = t1 - t0
+                timing["gradients_s"] = time.perf_counter() - t1
             kinds = ["blast" if isinstance(p.params, BlastParams) else "shock_bubble" for p in problems]
             grads = [dict(zip(PARAM_NAMES[k], map(float, g))) for k, g in zip(kinds, dJ)]
             return [float(x) for x in J], grads, dts, b

@@ -33,6 +33,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "lanes.cuh"
+
 
 namespace eu {
 
@@ -116,6 +118,23 @@ template <class T> __device__ __forceinline__ T gm1() { return T(kGm1D); }
 template <class T> __device__ __forceinline__ T inv_gm1() { return T(1.0 / kGm1D); }
 template <class T> __device__ __forceinline__ T gam() { return T(kGammaD); }
 
+// Arithmetic of the full-logic path (cell_full and the functions it calls).
+// FP64 keeps plain operators (fused by the compiler, within the tolerance of
+// the FP64 parity tests).  FP32 fixes every rounding (lanes.cuh), so that a
+// flagged cell's bits do not depend on the kernel the call is compiled into:
+// the same cell may be recomputed in full by the x-sweep, by either y-sweep
+// pass or by an ensemble task, and must come out the same from each.
+template <class T> __device__ __forceinline__ T xadd(T a, T b) { return a + b; }
+template <class T> __device__ __forceinline__ T xsub(T a, T b) { return a - b; }
+template <class T> __device__ __forceinline__ T xmul(T a, T b) { return a * b; }
+template <class T> __device__ __forceinline__ T xfma(T a, T b, T c) { return a * b + c; }   // a b + c
+template <class T> __device__ __forceinline__ T xfms(T a, T b, T c) { return c - a * b; }   // c - a b
+template <> __device__ __forceinline__ float xadd<float>(float a, float b) { return vadd(a, b); }
+template <> __device__ __forceinline__ float xsub<float>(float a, float b) { return vsub(a, b); }
+template <> __device__ __forceinline__ float xmul<float>(float a, float b) { return vmul(a, b); }
+template <> __device__ __forceinline__ float xfma<float>(float a, float b, float c) { return vfma(a, b, c); }
+template <> __device__ __forceinline__ float xfms<float>(float a, float b, float c) { return vfma(-a, b, c); }
+
 // ---------------------------------------------------------------------------
 // head/physics.hpp:13-20  cons_to_prim (pressure recovery)
 // ---------------------------------------------------------------------------
@@ -136,20 +155,20 @@ template <> __device__ __forceinline__ Prim<double> cons_to_prim<double>(const C
 // 24-bit momenta, one IEEE division.  Taken only where the FP32 form would
 // cancel (kinetic > E/2), i.e. strong rarefactions and high-Mach flow.
 static __device__ __noinline__ float pressure_fp64(float r, float mn, float mt, float e) {
-    const double rd = r;
-    const double kin = 0.5 * ((double)mn * (double)mn + (double)mt * (double)mt) / rd;
-    return (float)(kGm1D * ((double)e - kin));
+    const double kin = __ddiv_rn(__dmul_rn(0.5, __fma_rn((double)mn, (double)mn, __dmul_rn((double)mt, (double)mt))),
+                                 (double)r);
+    return __double2float_rn(__dmul_rn(kGm1D, __dsub_rn((double)e, kin)));
 }
 
 template <> __device__ __forceinline__ Prim<float> cons_to_prim<float>(const Cons<float>& U) {
     Prim<float> V;
-    V.ir = Ar<float>::rcp(U.r);
+    V.ir = vrcp(U.r);
     V.r = U.r;
-    V.un = U.mn * V.ir;
-    V.ut = U.mt * V.ir;
-    const float kinetic = 0.5f * U.r * (V.un * V.un + V.ut * V.ut);
-    V.p = gm1<float>() * (U.e - kinetic);
-    if (__builtin_expect(2.0f * kinetic > U.e, 0)) V.p = pressure_fp64(U.r, U.mn, U.mt, U.e);
+    V.un = vmul(U.mn, V.ir);
+    V.ut = vmul(U.mt, V.ir);
+    const float kinetic = vmul(vmul(0.5f, U.r), vfma(V.un, V.un, vmul(V.ut, V.ut)));
+    V.p = vmul(gm1<float>(), vsub(U.e, kinetic));
+    if (__builtin_expect(vmul(2.0f, kinetic) > U.e, 0)) V.p = pressure_fp64(U.r, U.mn, U.mt, U.e);
     return V;
 }
 
@@ -157,10 +176,10 @@ template <> __device__ __forceinline__ Prim<float> cons_to_prim<float>(const Con
 template <class T> __device__ __forceinline__ Cons<T> prim_to_cons(const Prim<T>& V) {
     Cons<T> U;
     U.r = V.r;
-    U.mn = V.r * V.un;
-    U.mt = V.r * V.ut;
-    const T kinetic = T(0.5) * V.r * (V.un * V.un + V.ut * V.ut);
-    U.e = V.p * inv_gm1<T>() + kinetic;
+    U.mn = xmul(V.r, V.un);
+    U.mt = xmul(V.r, V.ut);
+    const T kinetic = xmul(xmul(T(0.5), V.r), xfma(V.un, V.un, xmul(V.ut, V.ut)));
+    U.e = xfma(V.p, inv_gm1<T>(), kinetic);
     return U;
 }
 
@@ -173,9 +192,9 @@ template <class T> __device__ __forceinline__ T sound_speed(const Prim<T>& V) {
 template <class T> __device__ __forceinline__ Cons<T> flux(const Cons<T>& U, const Prim<T>& V) {
     Cons<T> F;
     F.r = U.mn;
-    F.mn = U.mn * V.un + V.p;
-    F.mt = U.mt * V.un;
-    F.e = (U.e + V.p) * V.un;
+    F.mn = xfma(U.mn, V.un, V.p);
+    F.mt = xmul(U.mt, V.un);
+    F.e = xmul(xadd(U.e, V.p), V.un);
     return F;
 }
 
@@ -223,13 +242,13 @@ __device__ __forceinline__ Cons<T> hll_from(const Cons<T>& UL, const Cons<T>& UR
                                             const Cons<T>& FR, T SL, T SR) {
     if (SL >= T(0)) return FL;
     if (SR <= T(0)) return FR;
-    const T den = SR - SL;
+    const T den = xsub(SR, SL);
     if (Ar<T>::fabs_(den) < T(1.0e-14)) return c_avg(FL, FR);
-    const T id = Ar<T>::rcp(den), ss = SL * SR;
-    return Cons<T>{(SR * FL.r - SL * FR.r + ss * (UR.r - UL.r)) * id,
-                   (SR * FL.mn - SL * FR.mn + ss * (UR.mn - UL.mn)) * id,
-                   (SR * FL.mt - SL * FR.mt + ss * (UR.mt - UL.mt)) * id,
-                   (SR * FL.e - SL * FR.e + ss * (UR.e - UL.e)) * id};
+    const T id = Ar<T>::rcp(den), ss = xmul(SL, SR);
+    // (SR F_L - SL F_R + SL SR (U_R - U_L)) / (SR - SL)
+    auto h = [&](T fl, T fr, T ul, T ur) { return xmul(xfma(ss, xsub(ur, ul), xfms(SL, fr, xmul(SR, fl))), id); };
+    return Cons<T>{h(FL.r, FR.r, UL.r, UR.r), h(FL.mn, FR.mn, UL.mn, UR.mn), h(FL.mt, FR.mt, UL.mt, UR.mt),
+                   h(FL.e, FR.e, UL.e, UR.e)};
 }
 
 // head/riemann.hpp:87-129 (Davis wave speeds; central average for
@@ -240,8 +259,8 @@ __device__ __forceinline__ Cons<T> hll_flux(const Cons<T>& UL, const Prim<T>& VL
     const Cons<T> FL = flux(UL, VL), FR = flux(UR, VR);
     if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(FL, FR);
     const T aL = sound_speed(VL), aR = sound_speed(VR);
-    const T SL = Ar<T>::fmin_(VL.un - aL, VR.un - aR);
-    const T SR = Ar<T>::fmax_(VL.un + aL, VR.un + aR);
+    const T SL = Ar<T>::fmin_(xsub(VL.un, aL), xsub(VR.un, aR));
+    const T SR = Ar<T>::fmax_(xadd(VL.un, aL), xadd(VR.un, aR));
     return hll_from(UL, UR, FL, FR, SL, SR);
 }
 
@@ -254,14 +273,14 @@ __device__ __forceinline__ Cons<T> hllc_flux(const Cons<T>& UL, const Prim<T>& V
     if (!physical_riemann(VL) || !physical_riemann(VR)) return c_avg(FL, FR);
     const T aL = sound_speed(VL), aR = sound_speed(VR);
     const T unL = VL.un, unR = VR.un;
-    const T SL = Ar<T>::fmin_(unL - aL, unR - aR);
-    const T SR = Ar<T>::fmax_(unL + aL, unR + aR);
+    const T SL = Ar<T>::fmin_(xsub(unL, aL), xsub(unR, aR));
+    const T SR = Ar<T>::fmax_(xadd(unL, aL), xadd(unR, aR));
     if (SL >= T(0)) return FL;
     if (SR <= T(0)) return FR;
-    const T qL = VL.r * (SL - unL), qR = VR.r * (SR - unR);
-    const T numerator = VR.p - VL.p + qL * unL - qR * unR;
-    const T denominator = qL - qR;
-    const T Sstar = numerator * Ar<T>::rcp(denominator);
+    const T qL = xmul(VL.r, xsub(SL, unL)), qR = xmul(VR.r, xsub(SR, unR));
+    const T numerator = xfms(qR, unR, xfma(qL, unL, xsub(VR.p, VL.p)));
+    const T denominator = xsub(qL, qR);
+    const T Sstar = xmul(numerator, Ar<T>::rcp(denominator));
     if (Ar<T>::fabs_(denominator) < T(1.0e-14) || !Ar<T>::finite(Sstar))
         return hll_from(UL, UR, FL, FR, SL, SR);
     // Upwind side of the contact: one star state, selected without branching.
@@ -275,15 +294,16 @@ __device__ __forceinline__ Cons<T> hllc_flux(const Cons<T>& UL, const Prim<T>& V
     const T irho = left ? VL.ir : VR.ir;
     const T S = left ? SL : SR;
     // hllc_star_state (head/riemann.hpp:135-186): falls back to U itself
-    const T dS = S - Sstar;
-    const T q = rho * (S - un);
-    const T rho_star = q * Ar<T>::rcp(dS);
-    const T E_star = rho_star * (U.e * irho + (Sstar - un) * (Sstar + p * Ar<T>::rcp(q)));
+    const T dS = xsub(S, Sstar);
+    const T q = xmul(rho, xsub(S, un));
+    const T rho_star = xmul(q, Ar<T>::rcp(dS));
+    // E* = rho* (E/rho + (S* - u)(S* + p/q))
+    const T E_star = xmul(rho_star, xfma(U.e, irho, xmul(xsub(Sstar, un), xfma(p, Ar<T>::rcp(q), Sstar))));
     const bool ok = !(Ar<T>::fabs_(dS) < T(1.0e-14)) && Ar<T>::finite(rho_star) && rho_star > T(0) &&
                     Ar<T>::finite(E_star);
-    const Cons<T> Us = ok ? Cons<T>{rho_star, rho_star * Sstar, rho_star * ut, E_star} : U;
-    return Cons<T>{F.r + S * (Us.r - U.r), F.mn + S * (Us.mn - U.mn), F.mt + S * (Us.mt - U.mt),
-                   F.e + S * (Us.e - U.e)};
+    const Cons<T> Us = ok ? Cons<T>{rho_star, xmul(rho_star, Sstar), xmul(rho_star, ut), E_star} : U;
+    return Cons<T>{xfma(S, xsub(Us.r, U.r), F.r), xfma(S, xsub(Us.mn, U.mn), F.mn), xfma(S, xsub(Us.mt, U.mt), F.mt),
+                   xfma(S, xsub(Us.e, U.e), F.e)};
 }
 
 // head/riemann.hpp:284-325 (local-alpha FORCE)
@@ -294,15 +314,15 @@ __device__ __forceinline__ Cons<T> force_flux(const Cons<T>& UL, const Prim<T>& 
     const Cons<T> Fc = c_avg(FL, FR);
     if (!physical_riemann(VL) || !physical_riemann(VR)) return Fc;   // hll_flux -> central average
     const T aL = sound_speed(VL), aR = sound_speed(VR);
-    const T alpha = Ar<T>::fmax_(Ar<T>::fabs_(VL.un) + aL, Ar<T>::fabs_(VR.un) + aR);
+    const T alpha = Ar<T>::fmax_(xadd(Ar<T>::fabs_(VL.un), aL), xadd(Ar<T>::fabs_(VR.un), aR));
     if (!Ar<T>::finite(alpha) || alpha <= T(1.0e-14)) return Fc;
-    const T ha = T(0.5) * alpha;
-    const T hia = T(0.5) * Ar<T>::rcp(alpha);
-    const Cons<T> Flf{Fc.r - ha * (UR.r - UL.r), Fc.mn - ha * (UR.mn - UL.mn),
-                      Fc.mt - ha * (UR.mt - UL.mt), Fc.e - ha * (UR.e - UL.e)};
+    const T ha = xmul(T(0.5), alpha);
+    const T hia = xmul(T(0.5), Ar<T>::rcp(alpha));
+    const Cons<T> Flf{xfms(ha, xsub(UR.r, UL.r), Fc.r), xfms(ha, xsub(UR.mn, UL.mn), Fc.mn),
+                      xfms(ha, xsub(UR.mt, UL.mt), Fc.mt), xfms(ha, xsub(UR.e, UL.e), Fc.e)};
     const Cons<T> Ua = c_avg(UL, UR);
-    const Cons<T> Uri{Ua.r - hia * (FR.r - FL.r), Ua.mn - hia * (FR.mn - FL.mn),
-                      Ua.mt - hia * (FR.mt - FL.mt), Ua.e - hia * (FR.e - FL.e)};
+    const Cons<T> Uri{xfms(hia, xsub(FR.r, FL.r), Ua.r), xfms(hia, xsub(FR.mn, FL.mn), Ua.mn),
+                      xfms(hia, xsub(FR.mt, FL.mt), Ua.mt), xfms(hia, xsub(FR.e, FL.e), Ua.e)};
     const Prim<T> Vri = cons_to_prim(Uri);
     if (!physical_riemann(Vri)) return Flf;
     return c_avg(Flf, flux(Uri, Vri));
@@ -635,14 +655,13 @@ template <class T>
 __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc, const Prim<T>& Wp,
                                             T hl, Face<T>& L, Face<T>& R) {
     Prim<T> s;
-    s.r = minmod(Wc.r - Wm.r, Wp.r - Wc.r);
-    s.un = minmod(Wc.un - Wm.un, Wp.un - Wc.un);
-    s.ut = minmod(Wc.ut - Wm.ut, Wp.ut - Wc.ut);
-    s.p = minmod(Wc.p - Wm.p, Wp.p - Wc.p);
-    Prim<T> WL{Wc.r - T(0.5) * s.r, Wc.un - T(0.5) * s.un, Wc.ut - T(0.5) * s.ut, Wc.p - T(0.5) * s.p,
-               T(0)};
-    Prim<T> WR{Wc.r + T(0.5) * s.r, Wc.un + T(0.5) * s.un, Wc.ut + T(0.5) * s.ut, Wc.p + T(0.5) * s.p,
-               T(0)};
+    s.r = minmod(xsub(Wc.r, Wm.r), xsub(Wp.r, Wc.r));
+    s.un = minmod(xsub(Wc.un, Wm.un), xsub(Wp.un, Wc.un));
+    s.ut = minmod(xsub(Wc.ut, Wm.ut), xsub(Wp.ut, Wc.ut));
+    s.p = minmod(xsub(Wc.p, Wm.p), xsub(Wp.p, Wc.p));
+    const T h = T(0.5);
+    Prim<T> WL{xfms(h, s.r, Wc.r), xfms(h, s.un, Wc.un), xfms(h, s.ut, Wc.ut), xfms(h, s.p, Wc.p), T(0)};
+    Prim<T> WR{xfma(h, s.r, Wc.r), xfma(h, s.un, Wc.un), xfma(h, s.ut, Wc.ut), xfma(h, s.p, Wc.p), T(0)};
     if (!physical_recon(WL)) WL = Wc;
     if (!physical_recon(WR)) WR = Wc;
     const Cons<T> UL = prim_to_cons(WL), UR = prim_to_cons(WR);
@@ -658,9 +677,10 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
         VUR = WR; VUR.ir = Ar<T>::rcp(WR.r);
     }
     const Cons<T> FL = flux(UL, VUL), FR = flux(UR, VUR);
-    const Cons<T> h{hl * (FR.r - FL.r), hl * (FR.mn - FL.mn), hl * (FR.mt - FL.mt), hl * (FR.e - FL.e)};
-    const Cons<T> cl{UL.r - h.r, UL.mn - h.mn, UL.mt - h.mt, UL.e - h.e};
-    const Cons<T> cr{UR.r - h.r, UR.mn - h.mn, UR.mt - h.mt, UR.e - h.e};
+    const Cons<T> d{xmul(hl, xsub(FR.r, FL.r)), xmul(hl, xsub(FR.mn, FL.mn)), xmul(hl, xsub(FR.mt, FL.mt)),
+                    xmul(hl, xsub(FR.e, FL.e))};
+    const Cons<T> cl{xsub(UL.r, d.r), xsub(UL.mn, d.mn), xsub(UL.mt, d.mt), xsub(UL.e, d.e)};
+    const Cons<T> cr{xsub(UR.r, d.r), xsub(UR.mn, d.mn), xsub(UR.mt, d.mt), xsub(UR.e, d.e)};
     const Prim<T> Vcl = cons_to_prim(cl), Vcr = cons_to_prim(cr);
     const bool okL = physical_recon(Vcl), okR = physical_recon(Vcr);
     L.U = okL ? cl : UL;
@@ -1019,19 +1039,23 @@ template <class T> __device__ __forceinline__ T signal_speed_fast(const Cons<T>&
     return Ar<T>::fmax_(Ar<T>::fabs_(U.mn), Ar<T>::fabs_(U.mt)) * ir + a;
 }
 
-// FP32 signal speeds of two states at once for the CFL reduction:
+// FP32 signal speed for the CFL reduction in lane form (lanes.cuh):
 // max(|u_n|, |u_t|) + a = (max(|m_n|, |m_t|) + rho a) / rho with
 // (rho a)^2 = gamma (gamma-1) (rho E - |m|^2/2), so the pressure needs no
-// division; the shared operations run as f32x2 pairs.  NaN (or +inf) for
-// a non-finite or negative-pressure state, as signal_speed_fast.
+// division.  NaN (or +inf) for a non-finite or negative-pressure state, as
+// signal_speed_fast.  Every FP32 y-sweep pass takes this form, one cell
+// (V = float) or two rows at a time (V = F2) with every rounding explicit,
+// so that a cell's speed, and with it the step's dt, does not depend on
+// which pass computed the cell.
+template <class V> __device__ __forceinline__ V speed_v(const Cons<V>& U) {
+    const V m2 = vfma(U.mt, U.mt, vmul(U.mn, U.mn));
+    const V q = vfma(splat<V>(-0.5f), m2, vmul(U.e, U.r));
+    const V ra = vsqrt(vmul(splat<V>(float(kGammaD * kGm1D)), q));
+    return vmul(vadd(vmax(vabs(U.mn), vabs(U.mt)), ra), vrcp(U.r));
+}
 __device__ __forceinline__ float2 signal_speed_rows(const Cons<float>& A, const Cons<float>& B) {
-    const float2 mn = f2(A.mn, B.mn), mt = f2(A.mt, B.mt);
-    const float2 m2 = __ffma2_rn(mt, mt, __fmul2_rn(mn, mn));
-    const float2 q = __ffma2_rn(f2s(-0.5f), m2, __fmul2_rn(f2(A.e, B.e), f2(A.r, B.r)));
-    const float2 x = __fmul2_rn(f2s(float(kGammaD * kGm1D)), q);
-    const float2 ra = f2(Ar<float>::sqrt_(x.x), Ar<float>::sqrt_(x.y));
-    const float2 mx = f2(fmaxf(fabsf(A.mn), fabsf(A.mt)), fmaxf(fabsf(B.mn), fabsf(B.mt)));
-    return __fmul2_rn(__fadd2_rn(mx, ra), f2(Ar<float>::rcp(A.r), Ar<float>::rcp(B.r)));
+    const F2 sp = speed_v(Cons<F2>{mk2(A.r, B.r), mk2(A.mn, B.mn), mk2(A.mt, B.mt), mk2(A.e, B.e)});
+    return make_float2(lo(sp), hi(sp));
 }
 
 // Full-logic recomputation of one cell (out of line; taken only by lanes

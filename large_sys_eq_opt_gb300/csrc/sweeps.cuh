@@ -671,7 +671,9 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
                     Nprev = N;
                 }
             } else {
-                const T sp = signal_speed_fast(N);
+                T sp;
+                if constexpr (sizeof(T) == 4) sp = speed_v<float>(N);   // the fast pass's form, per cell
+                else sp = signal_speed_fast(N);
                 if (out_ok) {
                     if constexpr (sizeof(T) == 4) {
                         smax = max_nan(smax, sp);     // NaN propagates: checked once at the end

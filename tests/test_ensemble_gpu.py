@@ -33,8 +33,10 @@ def small_ensemble():
 
 
 @pytest.mark.parametrize("prec,solver", [("fp32", "hllc"), ("fp64", "hllc"), ("fp32", "exact"),
-                                         ("fp32", "force"), ("fp64", "hll")])
+                                         ("fp32", "force"), ("fp32", "hll"), ("fp64", "hll")])
 def test_ensemble_matches_single_runs(E, prec, solver):
+    """Every instance of an uneven ensemble equals its own handle's run to
+    t_end bit for bit (steps, time and state)."""
     probs = small_ensemble()
     with E.Batch(probs, prec, solver) as b:
         b.start()

@@ -711,6 +711,16 @@ __device__ __forceinline__ void reconstruct(const Prim<T>& Wm, const Prim<T>& Wc
 template <class T> __device__ __forceinline__ bool phys_above(const Prim<T>& V, T floor) {
     return (V.r > floor) & (V.p > floor);
 }
+// FP32: min(rho, p) > floor with a NaN-propagating min (PTX min.NaN) is the
+// pair of tests above, NaN included, in one fewer instruction.
+__device__ __forceinline__ float min_nan(float a, float b) {
+    float d;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+template <> __device__ __forceinline__ bool phys_above<float>(const Prim<float>& V, float floor) {
+    return min_nan(V.r, V.p) > floor;
+}
 // FP64: the same tests on the integer pipes (Ar<double>::gt).
 template <> __device__ __forceinline__ bool phys_above<double>(const Prim<double>& V, double floor) {
     return Ar<double>::gt(V.r, floor) & Ar<double>::gt(V.p, floor);
@@ -930,7 +940,8 @@ __device__ __forceinline__ void reconstruct_fast<float>(const Prim<float>& dm, c
     L.V = Prim<float>{cr.x, vun.x, vut.x, vp.x, ir.x};
     R.V = Prim<float>{cr.y, vun.y, vut.y, vp.y, ir.y};
     slow |= (t.x > ce.x) | (t.y > ce.y);          // FP64 pressure island (c2p_fast)
-    slow |= !(nice && phys_recon_fast(L.V) && phys_recon_fast(R.V));
+    // phys_recon_fast(L.V) && phys_recon_fast(R.V) as one NaN-propagating min
+    slow |= !(nice && min_nan(min_nan(cr.x, vp.x), min_nan(cr.y, vp.y)) > float(kRhoFloorD));
 }
 
 template <class T> __device__ __forceinline__ Cons<T> nflux(const Cons<T>& U, const Prim<T>& V) {
@@ -989,7 +1000,10 @@ __device__ __forceinline__ Cons<T> hllc_fast(const Cons<T>& UL, const Prim<T>& V
     const T E_star = (sK * U.e + (Sstar - un) * (q * Sstar + p)) * idS;
     const bool upL = SL >= T(0), upR = SR <= T(0);
     const T Se = (upL || upR) ? T(0) : S;
-    const bool ok = !(Ar<T>::fabs_(denominator) < T(1.0e-14)) && !(Ar<T>::fabs_(dS) < T(1.0e-14)) &&
+    // !(|den| < 1e-14) && !(|dS| < 1e-14) as one test of the smaller
+    // magnitude: fmin returns the other argument for one NaN, and a NaN
+    // passes its own test, so the two forms agree for every input
+    const bool ok = !(Ar<T>::fmin_(Ar<T>::fabs_(denominator), Ar<T>::fabs_(dS)) < T(1.0e-14)) &&
                     Ar<T>::fabs_(Sstar + rho_star + E_star) < T(INFINITY) && rho_star > T(0) &&
                     !(upL && !left) && !(upR && left);
     slow |= !ok;

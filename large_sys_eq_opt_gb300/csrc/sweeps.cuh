@@ -131,12 +131,15 @@ template <class T, int S> struct Line {
     // The fast path only, with the cell's primitives W given (c2p_fast of U,
     // computed ahead for two rows at a time) and one flag for every
     // fallback the push could need (the cell's FP64 pressure island included
-    // by the caller); the y-sweep's fast pass.
+    // by the caller); the y-sweep's fast pass.  The previous right face is
+    // physical after every push of this path, so the one flag rp_phys can
+    // raise -- a line whose first state fails phys_riemann_fast -- is the
+    // caller's to raise once, after prime().
     __device__ __forceinline__ Cons<T> step_fast(const Cons<T>& U, const Prim<T>& W, T hl, T lam, bool& flag) {
         const bool nice = nice_cell(W);
         Face<T> L, R;
         Prim<T> dp;
-        bool slow = !rp_phys;
+        bool slow = false;
         reconstruct_fast(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow, dp);
         const Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);
         flag |= slow;
@@ -147,7 +150,6 @@ template <class T, int S> struct Line {
         Um1 = U;
         Rp = R;
         nice2 = nice1; nice1 = nice;
-        rp_phys = true;
         return N;
     }
 };
@@ -611,15 +613,16 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
         const unsigned live_mask = nlive >= RY ? (1u << RY) - 1u : (nlive > 0 ? (1u << nlive) - 1u : 0u);
         const int nout = k == 0 ? 0 : min(RY, e - ir0);
         const unsigned out_mask = !col_ok ? 0u : (nout >= RY ? (1u << RY) - 1u : (nout > 0 ? (1u << nout) - 1u : 0u));
-        bool flag = false;
-        if (k == 0) {   // window of the line's first cell (see Line::prime)
-            line.prime(Cons<T>{sb[0], sb[2 * RY * BW], sb[RY * BW], sb[3 * RY * BW]});
-        }
         // FP32 fast pass: the box's cells are converted to primitives two
         // rows at a time (packed), and the outputs' signal speeds likewise
         // (not for the exact solver, whose register-heavy Riemann call
         // spilled with four rows' primitives held ahead)
         constexpr bool kRows = FAST && sizeof(T) == 4 && S != kExact;
+        bool flag = false;
+        if (k == 0) {   // window of the line's first cell (see Line::prime)
+            line.prime(Cons<T>{sb[0], sb[2 * RY * BW], sb[RY * BW], sb[3 * RY * BW]});
+            if constexpr (kRows) flag = !line.rp_phys;   // step_fast's first push (box 0 is all live)
+        }
         Cons<T> Ub[RY];
         Prim<T> Wb[RY];
         bool ib[RY];

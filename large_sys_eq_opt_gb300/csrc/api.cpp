@@ -529,13 +529,15 @@ int eu_time_steps(eu_handle* h, int nsteps, int use_graph, float ms[3]) {
 int eu_autotune(eu_handle* h, int steps, long long chosen[2]) {
     Range range_("eu_autotune");
     if (!h || steps < 1) return fail(h, EU_ERR_INVALID, "eu_autotune: bad argument");
-    const int CX = h->K.box_x, RY = h->K.ry;
+    const int CX = h->K.box_x, RY = kYLag;        // y segments: whole output boxes
     // the current shape first: it is kept unless a candidate beats it by 1%
     std::vector<int> cx{h->seg_x}, cy{h->seg_y};
     for (int v : {CX, 2 * CX, 4 * CX, 32, 64, 128, 256})
         if (v % CX == 0 && v <= round_up(h->cfg.nx, CX) && std::find(cx.begin(), cx.end(), v) == cx.end()) cx.push_back(v);
-    for (int v : {RY, 2 * RY, 4 * RY, 32, 64, 128})
-        if (v % RY == 0 && v <= round_up(h->cfg.ny, RY) && std::find(cy.begin(), cy.end(), v) == cy.end()) cy.push_back(v);
+    // the planner's neighbours keep its remainder modulo the input box height
+    for (int v : {RY, 2 * RY, 4 * RY, 32, 64, 128, h->seg_y - 2 * RY, h->seg_y + 2 * RY})
+        if (v >= RY && v % RY == 0 && v <= round_up(h->cfg.ny, RY) && std::find(cy.begin(), cy.end(), v) == cy.end())
+            cy.push_back(v);
     if (cx.empty()) cx.push_back(CX);
     if (cy.empty()) cy.push_back(RY);
     void* saved = nullptr;
@@ -636,7 +638,7 @@ int eu_set_option(eu_handle* h, const char* name, long long value) {
         h->ntasks_x = ((h->cfg.ny + 31) / 32) * h->nseg_x;
         h->ctas_x = (h->ntasks_x + h->K.nw - 1) / h->K.nw;
     } else if (k == "seg_y") {
-        if (value < h->K.ry || value % h->K.ry) return fail(h, EU_ERR_INVALID, "seg_y must be a multiple of the box height");
+        if (value < kYLag || value % kYLag) return fail(h, EU_ERR_INVALID, "seg_y must be a multiple of 4 rows");
         h->seg_y = (int)value;
         h->ntasks_y = h->nseg_y * ((h->cfg.ny + h->seg_y - 1) / h->seg_y);
         h->ctas_y = (h->ntasks_y + h->K.nw - 1) / h->K.nw;
@@ -655,6 +657,10 @@ int eu_set_option(eu_handle* h, const char* name, long long value) {
             }
             h->solver = (int)value;
             h->K = kernels_for(h->prec, h->solver);
+            // the solvers' y-sweeps load boxes of different heights (8 or 4
+            // rows): re-encode the maps that carry the box
+            if (h->K.ry != h->tm_y_ry)
+                if (int rc = encode_all(h)) return rc;
             plan(h);
         }
     } else {

@@ -24,7 +24,7 @@ int enc_state(eu_handle* h, void* b, CUtensorMap* xin, CUtensorMap* yout) {
     if (int rc = encode(h, xin, b, h->cfg.nx + kSOff + 2, h->pitch_s, h->plane_s, h->K.box_x, 32,
                         CU_TENSOR_MAP_SWIZZLE_32B, h->l2promo_x))
         return rc;
-    return encode(h, yout, b, wclip_of(h), h->pitch_s, h->plane_s, 32, h->K.ry, CU_TENSOR_MAP_SWIZZLE_NONE, 256);
+    return encode(h, yout, b, wclip_of(h), h->pitch_s, h->plane_s, 32, kYLag, CU_TENSOR_MAP_SWIZZLE_NONE, 256);
 }
 int enc_tmp(eu_handle* h, void* b, CUtensorMap* xout, CUtensorMap* yin) {
     if (int rc = encode(h, xout, b, h->cfg.nx + kTOff, h->pitch_t, h->plane_t, h->K.box_x, 32,
@@ -92,6 +92,12 @@ int adj_prepare(eu_handle* h, long long nsteps, int k) {
         for (auto& e : A.ev) EU_CUDA(h, cudaEventCreate(&e));
         A.k = k;
         A.nseg = nseg;
+        A.q_y_ry = h->K.ry;
+    }
+    if (A.q_y_ry != h->K.ry) {   // the solver changed since the ring was built: boxes of other heights
+        for (int j = 0; j < k; ++j)
+            if (int rc = enc_tmp(h, A.Q[j], &A.Q_xo[j], &A.Q_y[j])) return rc;
+        A.q_y_ry = h->K.ry;
     }
     A.nseg = nseg;
     if (nsteps > A.dts_cap) {
@@ -117,6 +123,7 @@ int adj_prepare(eu_handle* h, long long nsteps, int k) {
 // of step j writes Q[j], the y-sweep writes R[j+1] (ck[s+1] for the last).
 template <class T> cudaError_t adj_segment_t(eu_handle* h, int s) {
     auto& A = h->adj;
+    if (A.q_y_ry != h->K.ry) return cudaErrorInvalidValue;   // see launch_y
     const long long n0 = (long long)s * A.k;
     const int len = (int)std::min<long long>(A.k, A.nsteps - n0);
     Ctl& c = A.hctl[s];

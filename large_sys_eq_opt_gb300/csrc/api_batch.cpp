@@ -29,6 +29,7 @@ template <class T> int batch_build_t(eu_batch* b) {
     int tx = 0, ty = 0;
     for (int i = 0; i < b->n; ++i) {
         eu_handle* h = b->h[(size_t)i];
+        if (h->tm_y_ry != b->K.ry) return bfail(b, EU_ERR_INVALID, "ensemble: an instance's y map has another box height");
         EnsInst<T>& I = inst[(size_t)i];
         I.tm_x[0] = h->tm_x[0];
         I.tm_x[1] = h->tm_x[1];
@@ -241,7 +242,7 @@ int eu_batch_time_steps(eu_batch* b, int nsteps, float* ms) {
 // and control blocks are restored afterwards.
 int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]) {
     if (!b || steps < 1) return bfail(b, EU_ERR_INVALID, "bad argument");
-    const int CX = b->K.box_x, RY = b->K.ry;
+    const int CX = b->K.box_x, RY = kYLag;        // y segments: whole output boxes
     std::vector<void*> saved((size_t)b->n, nullptr);
     std::vector<Ctl> ctl0((size_t)b->n);
     std::vector<int> cur0((size_t)b->n);

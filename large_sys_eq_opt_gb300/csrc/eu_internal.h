@@ -54,6 +54,11 @@ enum { kStatusOk = 0, kStatusNonPhysical = 1, kStatusTimeout = 2, kStatusNonFini
 // costs an ECC read-modify-write).
 constexpr int kSOff = 6;
 constexpr int kTOff = 8;
+// y-sweep: a cell is final 4 rows after it enters a line's stencil window
+// (2 ghost rows + 2 cells of lag), so its outputs are stored in boxes of 4
+// rows and row segments are multiples of 4 rows; the input boxes hold one or
+// more such groups of rows.
+constexpr int kYLag = 4;
 
 // SoA plane set: field f (0 rho, 1 rhou, 2 rhov, 3 E), array row r, column c
 // at base[f*plane + r*pitch + c].

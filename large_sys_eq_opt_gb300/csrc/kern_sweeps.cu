@@ -37,17 +37,23 @@ using T = double;
 constexpr int MINB_X = 2, MINB_Y = 2;
 #endif
 // x: boxes of 32 rows x 32 bytes x 4 fields (4 KB), 3 stages per warp.
-// y: boxes of 32 columns x RY rows x 4 fields, 3 stages per warp.
+// y: boxes of 36 columns x RY rows x 4 fields; FP32 8 rows in 2 stages per
+// warp (the per-box work halved, 4 CTAs per SM still fit), FP64 and the FP32
+// exact solver 4 rows in 3 (the exact solver's y-sweep spilled with 8-row
+// boxes: 27.0 -> 35.9 ms per step on the developed 8192^2 blast).
 constexpr int CX = 32 / sizeof(T);
 constexpr int SX = 3;
-constexpr int RY = 4, SY = 3;
+#ifndef EU_Y_ROWS
+#define EU_Y_ROWS (EU_PREC == 32 && EU_SOLVER != 2 ? 8 : 4)
+#endif
+constexpr int RY = EU_Y_ROWS, SY = RY == 8 ? 2 : 3;
 constexpr int BWY = 36;                 // y-sweep box width: the warp's 32 columns + 2, rounded to 16 B
 constexpr int NW = 4;
 constexpr int SOL = EU_SOLVER;
 constexpr size_t kStageX = 4 * 32 * CX * sizeof(T);
 constexpr size_t kStageY = (4 * RY * BWY * sizeof(T) + 127) / 128 * 128;
 constexpr size_t kSmemX = 1024 + NW * SX * kStageX + NW * SX * sizeof(uint64_t);
-constexpr size_t kOStageY = 4 * RY * 32 * sizeof(T);
+constexpr size_t kOStageY = 4 * kYLag * 32 * sizeof(T);
 constexpr size_t kSmemY = 1024 + NW * (SY * kStageY + 2 * kOStageY) + NW * SY * sizeof(uint64_t);
 
 static cudaError_t LAUNCH_X(const CUtensorMap* tm, const CUtensorMap* tm_out, const void* args, int ctas,

@@ -65,6 +65,7 @@ struct eu_handle {
     long long dtlog_cap = 0;
     CUtensorMap tm_x[2];
     CUtensorMap tm_y;
+    int tm_y_ry = 0;       // rows of tm_y's box: the y-sweep launch must expect exactly these (K.ry)
     CUtensorMap tm_xo;     // x-sweep output: Utmp boxes, rows [0, ny+2), columns [0, nx+kTOff)
     CUtensorMap tm_yo[2];  // y-sweep output: S boxes, columns [0, nx+kSOff) (right ghosts clipped)
     eu::SweepKernels K{};
@@ -86,6 +87,7 @@ struct eu_handle {
         std::vector<void*> R;    // k states: R[j] = state after s*k+j steps (j >= 1) of the ring segment
         std::vector<void*> Q;    // k x-sweep outputs of the ring segment
         std::vector<CUtensorMap> ck_x, ck_yo, R_x, R_yo, Q_xo, Q_y;
+        int q_y_ry = 0;          // rows of the Q_y boxes (K.ry when they were encoded)
         void* lam = nullptr;     // adjoint of the state
         void* mu = nullptr;      // adjoint of the x-sweep output
         double* d_dts = nullptr;

@@ -19,7 +19,7 @@
 // shared memory with TMA (cp.async.bulk.tensor.3d) while the warp computes.
 //   x-sweep : 32 rows per warp; boxes of 32 rows x 32 bytes, stored with the
 //             32-byte swizzle so that 16-byte row reads are bank-conflict free.
-//   y-sweep : 32 columns per warp; boxes of 32 columns x RY rows.  Its
+//   y-sweep : 32 columns per warp; boxes of 36 columns x RY rows.  Its
 //             epilogue reduces the maximum signal speed (warp shuffle max ->
 //             one atomic per warp) and the last warp to finish computes the
 //             next dt on the device.
@@ -40,14 +40,14 @@ namespace eu {
 // fluxes (src/cpu/solver_cpu.cpp:452-453, :489-490).
 template <class T, int S> struct Line {
     Prim<T> dm, Wm1;    // W(c-1) - W(c-2), primitives of cell c-1 (1/rho unused)
-    Cons<T> Um1;        // conserved state of cell c-1
-    Cons<T> A;          // U(c-2) + lam F(c-5/2): the update of cell c-2 less its right flux
+    Cons<T> Um1, Um2;   // conserved states of cells c-1 and c-2
+    Cons<T> Fm;         // flux F(c-5/2) through the left face of cell c-2
     Face<T> Rp;         // evolved right face state of cell c-2
     bool nice2, nice1;  // cells c-2, c-1 pass nice_cell()
     bool rp_phys;       // Rp is physical (always true when it came from the fast path)
 
     __device__ __forceinline__ void reset() {
-        dm = Prim<T>{}; Wm1 = Prim<T>{}; Um1 = Cons<T>{}; A = Cons<T>{};
+        dm = Prim<T>{}; Wm1 = Prim<T>{}; Um1 = Cons<T>{}; Um2 = Cons<T>{}; Fm = Cons<T>{};
         Rp = Face<T>{};
         nice2 = nice1 = false;
         rp_phys = false;
@@ -62,15 +62,35 @@ template <class T, int S> struct Line {
         const Prim<T> W = c2p_fast(U0, isl);
         dm = Prim<T>{}; Wm1 = W;
         Um1 = U0;
-        A = U0;
+        Um2 = U0;
+        Fm = Cons<T>{};
         Rp.U = U0;
         Rp.V = W;
         nice2 = nice1 = nice_cell(W);
         rp_phys = phys_riemann_fast(W);
     }
 
-    // U(c-2) - lam (F(c-3/2) - F(c-5/2)) is evaluated as A - lam F(c-3/2)
-    // (src/cpu/solver_cpu.cpp:452-453, :489-490).
+    // The conservative update of cell c-2, U(c-2) - lam (F(c-3/2) - F(c-5/2))
+    // (src/cpu/solver_cpu.cpp:452-453, :489-490), in the reference's order
+    // of operations: equal fluxes leave a cell's state exactly as it was, so
+    // a uniform region stays uniform to the last bit (the exact solver's
+    // identical-states route depends on that).  Shifts the window's
+    // conserved states on to cell c.
+    __device__ __forceinline__ Cons<T> update(const Cons<T>& F, T lam, const Cons<T>& U) {
+        Cons<T> N;
+        if constexpr (sizeof(T) == 4) {
+            const float nl = -lam;
+            N = Cons<T>{vfma(nl, vsub(F.r, Fm.r), Um2.r), vfma(nl, vsub(F.mn, Fm.mn), Um2.mn),
+                        vfma(nl, vsub(F.mt, Fm.mt), Um2.mt), vfma(nl, vsub(F.e, Fm.e), Um2.e)};
+        } else {
+            N = Cons<T>{Um2.r - lam * (F.r - Fm.r), Um2.mn - lam * (F.mn - Fm.mn), Um2.mt - lam * (F.mt - Fm.mt),
+                        Um2.e - lam * (F.e - Fm.e)};
+        }
+        Fm = F;
+        Um2 = Um1;
+        Um1 = U;
+        return N;
+    }
     // SLOW = true: a cell flagged by its own reconstruction is recomputed in
     // full; a cell whose only flag is the face (a non-physical left face
     // state, a Riemann fallback) keeps its fast-path primitives and face
@@ -114,11 +134,9 @@ template <class T, int S> struct Line {
             fc |= slow_cell;
             ff |= slow_face;
         }
-        const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
-        A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
+        const Cons<T> N = update(F, lam, U);
         dm = dnext;
         Wm1 = W;
-        Um1 = U;
         Rp = R;
         nice2 = nice1; nice1 = nice;
         rp_phys = r_phys;
@@ -131,10 +149,9 @@ template <class T, int S> struct Line {
     // The fast path only, with the cell's primitives W given (c2p_fast of U,
     // computed ahead for two rows at a time) and one flag for every
     // fallback the push could need (the cell's FP64 pressure island included
-    // by the caller); the y-sweep's fast pass.  The previous right face is
-    // physical after every push of this path, so the one flag rp_phys can
-    // raise -- a line whose first state fails phys_riemann_fast -- is the
-    // caller's to raise once, after prime().
+    // by the caller); the y-sweep's fast pass, after warm4().  The previous
+    // right face is then always a physical one from reconstruct_fast, so the
+    // flag rp_phys carries for the full path is not needed here.
     __device__ __forceinline__ Cons<T> step_fast(const Cons<T>& U, const Prim<T>& W, T hl, T lam, bool& flag) {
         const bool nice = nice_cell(W);
         Face<T> L, R;
@@ -143,14 +160,48 @@ template <class T, int S> struct Line {
         reconstruct_fast(dm, Wm1, W, hl, nice && nice1 && nice2, L, R, slow, dp);
         const Cons<T> F = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);
         flag |= slow;
-        const Cons<T> N{A.r - lam * F.r, A.mn - lam * F.mn, A.mt - lam * F.mt, A.e - lam * F.e};
-        A = Cons<T>{Um1.r + lam * F.r, Um1.mn + lam * F.mn, Um1.mt + lam * F.mt, Um1.e + lam * F.e};
+        const Cons<T> N = update(F, lam, U);
         dm = dp;
         Wm1 = W;
-        Um1 = U;
         Rp = R;
         nice2 = nice1; nice1 = nice;
         return N;
+    }
+    // The four warm-up pushes of a line primed at row r0-2 (rows r0-2 .. r0+1,
+    // primitives W = c2p_fast(U) given), doing only the work that reaches an
+    // output: the first output (row r0, at the next push) needs the slopes
+    // W(r0-1) - W(r0-2) and W(r0) - W(r0-1), the reconstructions of cells
+    // r0-1 and r0 and the flux F(r0-1/2).  The reconstructions of cells r0-3
+    // and r0-2 start from the primed copy, and the fluxes F(r0-7/2) ..
+    // F(r0-3/2) and the updates of rows r0-4 .. r0-1 only feed outputs the
+    // task does not store, so they are skipped together with their fallback
+    // flags; the window then holds what four step_fast pushes leave in it.
+    __device__ __forceinline__ void warm4(const Cons<T> (&U)[4], const Prim<T> (&W)[4], T hl, bool& flag) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const bool nice = nice_cell(W[q]);
+            dm = Prim<T>{W[q].r - Wm1.r, W[q].un - Wm1.un, W[q].ut - Wm1.ut, W[q].p - Wm1.p, T(0)};
+            Wm1 = W[q];
+            Um2 = Um1;
+            Um1 = U[q];
+            nice2 = nice1; nice1 = nice;
+        }
+#pragma unroll
+        for (int q = 2; q < 4; ++q) {
+            const bool nice = nice_cell(W[q]);
+            Face<T> L, R;
+            Prim<T> dp;
+            bool slow = false;
+            reconstruct_fast(dm, Wm1, W[q], hl, nice && nice1 && nice2, L, R, slow, dp);
+            if (q == 3) Fm = riemann_fast<S>(Rp.U, Rp.V, L.U, L.V, slow);   // F(r0-1/2)
+            flag |= slow;
+            dm = dp;
+            Wm1 = W[q];
+            Um2 = Um1;
+            Um1 = U[q];
+            Rp = R;
+            nice2 = nice1; nice1 = nice;
+        }
     }
 };
 
@@ -390,14 +441,22 @@ __device__ __forceinline__ bool x_task(const CUtensorMap* tm, const CUtensorMap*
                 }
             }
         }
+        // Box 0 holds interior columns s0+2-CX .. s0+1; the first output
+        // (column s0, pushed with column s0+2) needs the window from column
+        // s0-2 on, so the line is primed there (as the y-sweep's) and the
+        // columns before it are not pushed at all (FP32: the first half of
+        // box 0).  A line started from nothing would also send its first two
+        // cells through the out-of-line full path.
+        constexpr int kWarmHalf = (CX - 4) / HV;
 #pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
+        for (int h = k == 0 ? kWarmHalf : 0; h < 2; ++h) {
             T* q = rowp + ((h ^ swz) * HV);
             T r[HV], mn[HV], mt[HV], en[HV];
             ld_vec<T, HV>(q, r);
             ld_vec<T, HV>(q + 32 * CX, mn);
             ld_vec<T, HV>(q + 64 * CX, mt);
             ld_vec<T, HV>(q + 96 * CX, en);
+            if (k == 0 && h == kWarmHalf) line.prime(Cons<T>{r[0], mn[0], mt[0], en[0]});
             if constexpr (sizeof(T) == 4 && S != kExact) {
                 // FP32: the cells' primitives two at a time (packed), then the
                 // pushes (not for the exact solver: it spilled)
@@ -512,11 +571,13 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 // y-sweep: Utmp -> Unew (S buffer), with the fused CFL reduction.  One warp
 // per (row segment, group of 32 S columns), one column per lane; the input
 // box is BW >= 34 Utmp columns wide because Utmp's interior sits two columns
-// right of the S interior.  Box k holds Utmp rows [r0 + 4k, r0 + 4k + 4);
-// a cell is final four rows after it enters, so box k >= 1 yields the output
-// rows [r0 + 4(k-1), r0 + 4k) of this segment (box 0 only warms the window
-// up); they are staged in shared memory and written with one TMA store of
-// whole 128-byte rows.  The store map ends at the last 16-byte boundary
+// right of the S interior.  Box k holds Utmp rows [r0 + RY k, r0 + RY k + RY)
+// (RY = 8 in FP32, 4 in FP64) and is processed in groups of 4 rows; a cell
+// is final four rows after it enters, so row group j+1 of the segment yields
+// the output rows [r0 + 4j, r0 + 4j + 4) (group 0 only warms the window up),
+// staged in shared memory and written with one TMA store of whole 128-byte
+// rows per group.  A box of 8 rows halves the per-box work (barrier wait,
+// TMA load, masks, abort vote) against boxes of 4.  The store map ends at the last 16-byte boundary
 // before the right ghost columns (TMA stores clip at 16-byte granularity);
 // columns past it, and group 0 whose box would also cover the left ghost
 // columns, are stored directly.
@@ -546,19 +607,22 @@ template <class T, int S, int RY, int BW, int STAGES, bool FAST>
 __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorMap* tm_out, const SweepArgs<T>& a,
                                           int task, T* buf, T* obuf, uint64_t* bar, uint32_t& phase, int lane,
                                           bool& aborted) {
-    constexpr int STAGE = 4 * RY * BW;
+    constexpr int LAG = kYLag;                   // rows of one output box
+    constexpr int HB = RY / LAG;                 // output boxes per input box
+    constexpr int STAGE = 4 * RY * BW;           // input box: 4 fields x RY rows x BW columns
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
-    constexpr int OSTAGE = 4 * RY * 32;          // output box: 4 fields x RY rows x 32 columns
+    constexpr int OSTAGE = 4 * LAG * 32;         // output box: 4 fields x LAG rows x 32 columns
     constexpr uint32_t OSTAGE_BYTES = OSTAGE * sizeof(T);
     static_assert(STAGE_BYTES % 128 == 0 && OSTAGE_BYTES % 128 == 0, "stage buffers must stay 128-byte aligned");
     static_assert(BW >= 32 + kTOff - kSOff, "box too narrow");
-    static_assert(RY == 4, "the 4-row output lag must be exactly one box");
+    static_assert(RY % LAG == 0, "an input box holds whole output boxes");
     Ctl* ctl = a.ctl;
     const int rs = task / a.nseg;                // row segment
     const int g = task - rs * a.nseg;            // group of 32 S columns
-    const int r0 = rs * a.seg;                   // first interior output row (a multiple of RY)
+    const int r0 = rs * a.seg;                   // first interior output row (a multiple of LAG)
     const int e = min(r0 + a.seg, a.ny);
-    const int nst = 1 + (e - r0 + RY - 1) / RY;  // warm-up box + output boxes
+    const int nob = (e - r0 + LAG - 1) / LAG;    // output boxes of this task
+    const int nst = ((nob + 1) * LAG + RY - 1) / RY;   // input boxes: LAG warm-up rows + the output rows
     const int sc = g * 32 + lane;                // S column of this lane
     const int i = sc - kSOff;                    // its interior column
     const bool col_ok = i >= 0 && i < a.nx;
@@ -599,109 +663,130 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
             kfail = k;
             break;
         }
-        const T* sb = buf + s * STAGE + lane + (kTOff - kSOff);
-        T* ob = obuf + (k & 1) * OSTAGE + lane;
-        if (k >= 3 && lane == 0) bulk_wait_read1();   // output buffer k&1 was stored at box k-2
-        __syncwarp();
-        const int ir0 = r0 + (k - 1) * RY;        // interior row of this box's first output
-        // Per-box masks over the box's rows (bit rr): pushes whose flags can
-        // reach an output (all of box 0, then up to the segment's last row),
-        // and pushes that yield an output of this task.  Testing a constant
-        // bit per unrolled row measured 2.6% faster than comparing row
-        // indices per cell.
-        const int nlive = k == 0 ? RY : e - ir0;
-        const unsigned live_mask = nlive >= RY ? (1u << RY) - 1u : (nlive > 0 ? (1u << nlive) - 1u : 0u);
-        const int nout = k == 0 ? 0 : min(RY, e - ir0);
-        const unsigned out_mask = !col_ok ? 0u : (nout >= RY ? (1u << RY) - 1u : (nout > 0 ? (1u << nout) - 1u : 0u));
-        // FP32 fast pass: the box's cells are converted to primitives two
-        // rows at a time (packed), and the outputs' signal speeds likewise
-        // (not for the exact solver, whose register-heavy Riemann call
-        // spilled with four rows' primitives held ahead)
+        const T* sbox = buf + s * STAGE + lane + (kTOff - kSOff);
+        // FP32 fast pass: the cells of a row group are converted to
+        // primitives two rows at a time (packed), and the outputs' signal
+        // speeds likewise (not for the exact solver, whose register-heavy
+        // Riemann call spilled with four rows' primitives held ahead)
         constexpr bool kRows = FAST && sizeof(T) == 4 && S != kExact;
         bool flag = false;
-        if (k == 0) {   // window of the line's first cell (see Line::prime)
-            line.prime(Cons<T>{sb[0], sb[2 * RY * BW], sb[RY * BW], sb[3 * RY * BW]});
-            if constexpr (kRows) flag = !line.rp_phys;   // step_fast's first push (box 0 is all live)
-        }
-        Cons<T> Ub[RY];
-        Prim<T> Wb[RY];
-        bool ib[RY];
-        if constexpr (kRows) {
-#pragma unroll
-            for (int rr = 0; rr < RY; ++rr) {
-                Ub[rr] = Cons<T>{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
-                ib[rr] = false;
-            }
-#pragma unroll
-            for (int rr = 0; rr < RY; rr += 2) c2p_rows(Ub[rr], Ub[rr + 1], Wb[rr], Wb[rr + 1], ib[rr], ib[rr + 1]);
-        }
-        Cons<T> Nprev{};
-#pragma unroll
-        for (int rr = 0; rr < RY; ++rr) {
-            // normal momentum of the y-sweep is rho*v (plane 2)
-            Cons<T> N;
+        if (k == 0)   // window of the line's first cell (see Line::prime)
+            line.prime(Cons<T>{sbox[0], sbox[2 * RY * BW], sbox[RY * BW], sbox[3 * RY * BW]});
+#pragma unroll 1
+        for (int h = 0; h < HB; ++h) {
+            const int j = k * HB + h - 1;         // output box of this row group (-1: warm-up)
+            if (j >= nob) break;                  // past the task's last output row (warp-uniform)
+            const T* sb = sbox + h * LAG * BW;    // the group's rows; fields RY * BW apart
+            T* ob = obuf + (j & 1) * OSTAGE + lane;
+            if (j >= 2 && lane == 0) bulk_wait_read1();   // output buffer j&1 was stored for box j-2
+            __syncwarp();
+            const int ir0 = r0 + j * LAG;         // interior row of this group's first output
+            // Masks over the group's rows (bit rr): pushes whose flags can
+            // reach an output (all of the warm-up group, then up to the
+            // segment's last row), and pushes that yield an output of this
+            // task.  Testing a constant bit per unrolled row measured 2.6%
+            // faster than comparing row indices per cell.
+            const int nlive = j < 0 ? LAG : e - ir0;
+            const unsigned live_mask = nlive >= LAG ? (1u << LAG) - 1u : (nlive > 0 ? (1u << nlive) - 1u : 0u);
+            const int nout = j < 0 ? 0 : min(LAG, e - ir0);
+            const unsigned out_mask =
+                !col_ok ? 0u : (nout >= LAG ? (1u << LAG) - 1u : (nout > 0 ? (1u << nout) - 1u : 0u));
+            Cons<T> Ub[LAG];
+            Prim<T> Wb[LAG];
+            bool ib[LAG];
             if constexpr (kRows) {
-                // a flag matters unless the push lies past the task's last
-                // output row (no later output depends on it)
-                bool f = ib[rr];
-                N = line.step_fast(Ub[rr], Wb[rr], hl, lam, f);
-                flag |= f & (((live_mask >> rr) & 1u) != 0u);
-            } else {
-                const Cons<T> U{sb[rr * BW], sb[(2 * RY + rr) * BW], sb[(RY + rr) * BW], sb[(3 * RY + rr) * BW]};
-                if constexpr (FAST) {
-                    bool fi = false, fc = false, ff = false;
-                    N = line.template step<false>(U, hl, lam, fi, fc, ff);
-                    flag |= (fi | fc | ff) & (((live_mask >> rr) & 1u) != 0u);
-                } else {
-                    N = line.push(U, hl, lam);
+#pragma unroll
+                for (int rr = 0; rr < LAG; ++rr) {
+                    Ub[rr] = Cons<T>{sb[rr * BW], sb[(2 * RY) * BW + rr * BW], sb[RY * BW + rr * BW],
+                                     sb[(3 * RY) * BW + rr * BW]};
+                    ib[rr] = false;
+                }
+#pragma unroll
+                for (int rr = 0; rr < LAG; rr += 2) c2p_rows(Ub[rr], Ub[rr + 1], Wb[rr], Wb[rr + 1], ib[rr], ib[rr + 1]);
+                if (j < 0) {   // the warm-up group (warp-uniform): every row's pressure island matters
+                    static_assert(LAG == 4, "warm4 takes the four warm-up rows");
+                    flag |= ib[0] | ib[1] | ib[2] | ib[3];
+                    line.warm4(Ub, Wb, hl, flag);
+                    continue;
                 }
             }
-            ob[rr * 32] = N.r;
-            ob[(RY + rr) * 32] = N.mt;
-            ob[(2 * RY + rr) * 32] = N.mn;
-            ob[(3 * RY + rr) * 32] = N.e;
-            const int ir = ir0 + rr;
-            const bool out_ok = ((out_mask >> rr) & 1u) != 0u;
-            if constexpr (kRows) {
-                if (rr & 1) {             // the speeds of rows rr-1 and rr
-                    // selects, not branches: a speed is >= 0 or NaN, so 0
-                    // stands in for a row without an output
-                    const float2 sp = signal_speed_rows(Nprev, N);
-                    const float s0 = ((out_mask >> (rr - 1)) & 1u) ? sp.x : 0.0f;
-                    const float s1 = out_ok ? sp.y : 0.0f;
-                    smax = max_nan(smax, max_nan(s0, s1));
+            Cons<T> Nprev{};
+#pragma unroll
+            for (int rr = 0; rr < LAG; ++rr) {
+                // normal momentum of the y-sweep is rho*v (plane 2)
+                Cons<T> N;
+                if constexpr (kRows) {
+                    // a flag matters unless the push lies past the task's
+                    // last output row (no later output depends on it)
+                    bool f = ib[rr];
+                    N = line.step_fast(Ub[rr], Wb[rr], hl, lam, f);
+                    flag |= f & (((live_mask >> rr) & 1u) != 0u);
                 } else {
-                    Nprev = N;
-                }
-            } else {
-                T sp;
-                if constexpr (sizeof(T) == 4) sp = speed_v<float>(N);   // the fast pass's form, per cell
-                else sp = signal_speed_fast(N);
-                if (out_ok) {
-                    if constexpr (sizeof(T) == 4) {
-                        smax = max_nan(smax, sp);     // NaN propagates: checked once at the end
+                    const Cons<T> U{sb[rr * BW], sb[(2 * RY) * BW + rr * BW], sb[RY * BW + rr * BW],
+                                    sb[(3 * RY) * BW + rr * BW]};
+                    if constexpr (FAST) {
+                        bool fi = false, fc = false, ff = false;
+                        N = line.template step<false>(U, hl, lam, fi, fc, ff);
+                        flag |= (fi | fc | ff) & (((live_mask >> rr) & 1u) != 0u);
                     } else {
-                        ssum += sp;                   // NaN / inf propagate: checked once at the end
-                        smax = Ar<T>::fmax_(smax, sp);
+                        N = line.push(U, hl, lam);
+                    }
+                }
+                ob[rr * 32] = N.r;
+                ob[(LAG + rr) * 32] = N.mt;
+                ob[(2 * LAG + rr) * 32] = N.mn;
+                ob[(3 * LAG + rr) * 32] = N.e;
+                const int ir = ir0 + rr;
+                const bool out_ok = ((out_mask >> rr) & 1u) != 0u;
+                if constexpr (kRows) {
+                    if (rr & 1) {             // the speeds of rows rr-1 and rr
+                        // selects, not branches: a speed is >= 0 or NaN, so
+                        // 0 stands in for a row without an output
+                        const float2 sp = signal_speed_rows(Nprev, N);
+                        const float s0 = ((out_mask >> (rr - 1)) & 1u) ? sp.x : 0.0f;
+                        const float s1 = out_ok ? sp.y : 0.0f;
+                        smax = max_nan(smax, max_nan(s0, s1));
+                    } else {
+                        Nprev = N;
+                    }
+                } else {
+                    T sp;
+                    if constexpr (sizeof(T) == 4) sp = speed_v<float>(N);   // the fast pass's form, per cell
+                    else sp = signal_speed_fast(N);
+                    if (out_ok) {
+                        if constexpr (sizeof(T) == 4) {
+                            smax = max_nan(smax, sp);     // NaN propagates: checked once at the end
+                        } else {
+                            ssum += sp;                   // NaN / inf propagate: checked once at the end
+                            smax = Ar<T>::fmax_(smax, sp);
+                        }
+                    }
+                }
+                if (special) {                        // warp-uniform: few warps store anything directly
+                    if (out_ok && direct) store_cell(a.out, ir + 2, sc, N, 2, 1, false);
+                    if (out_ok && edge) {             // x-ghost columns of Unew read by the next x-sweep
+                        if (i == 0) {
+                            if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
+                            else { store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, false);
+                                   store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, false); }
+                        }
+                        if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, true);
+                        if (i == a.nx - 1) {
+                            if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, true);
+                            else { store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, false);
+                                   store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, false); }
+                        }
+                        if (i == a.nx - 2 && a.bc_hi == kBcReflective)
+                            store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, true);
                     }
                 }
             }
-            if (special) {                        // warp-uniform: few warps store anything directly
-                if (out_ok && direct) store_cell(a.out, ir + 2, sc, N, 2, 1, false);
-                if (out_ok && edge) {             // x-ghost columns of Unew read by the next x-sweep
-                    if (i == 0) {
-                        if (a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, true);
-                        else { store_cell(a.out, ir + 2, kSOff - 1, N, 2, 1, false);
-                               store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, false); }
-                    }
-                    if (i == 1 && a.bc_lo == kBcReflective) store_cell(a.out, ir + 2, kSOff - 2, N, 2, 1, true);
-                    if (i == a.nx - 1) {
-                        if (a.bc_hi == kBcReflective) store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, true);
-                        else { store_cell(a.out, ir + 2, a.nx + kSOff, N, 2, 1, false);
-                               store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, false); }
-                    }
-                    if (i == a.nx - 2 && a.bc_hi == kBcReflective)
-                        store_cell(a.out, ir + 2, a.nx + kSOff + 1, N, 2, 1, true);
+            if (j >= 0) {   // store the group's outputs (an aborted pass's are rewritten by the full pass)
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0 && g != 0 && g * 32 < a.wclip) {
+                    tma_store_3d(tm_out, smem_u32(obuf + (j & 1) * OSTAGE), g * 32, ir0 + 2, 0);
+                    bulk_commit();
                 }
             }
         }
@@ -713,14 +798,8 @@ __device__ __forceinline__ YOut<T> y_pass(const CUtensorMap* tm, const CUtensorM
             }
         }
         fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-            if (k > 0 && g != 0 && g * 32 < a.wclip) {
-                tma_store_3d(tm_out, smem_u32(obuf + (k & 1) * OSTAGE), g * 32, ir0 + 2, 0);
-                bulk_commit();
-            }
-            if (k + STAGES < nst) issue(k + STAGES);
-        }
+        __syncwarp();                             // every lane is done with stage s
+        if (lane == 0 && k + STAGES < nst) issue(k + STAGES);
     }
     if (lane == 0) bulk_wait0();
     if (timed_out || aborted) {
@@ -765,7 +844,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
                    const SweepArgs<T> a) {
     constexpr int STAGE = 4 * RY * BW;
     constexpr uint32_t STAGE_BYTES = STAGE * sizeof(T);
-    constexpr int OSTAGE = 4 * RY * 32;
+    constexpr int OSTAGE = 4 * kYLag * 32;
     constexpr uint32_t OSTAGE_BYTES = OSTAGE * sizeof(T);
     extern __shared__ __align__(1024) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -836,7 +915,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) ensemble_kernel(const __grid_co
     constexpr int CX = 32 / sizeof(T);
     constexpr size_t XB = (size_t)SX * 4 * 32 * CX * sizeof(T);
     constexpr size_t YSTAGE = (size_t)4 * RY * BWY * sizeof(T);
-    constexpr size_t YB = SY * YSTAGE + 2 * (size_t)4 * RY * 32 * sizeof(T);
+    constexpr size_t YB = SY * YSTAGE + 2 * (size_t)4 * kYLag * 32 * sizeof(T);
     constexpr size_t WB = ((XB > YB ? XB : YB) + 1023) / 1024 * 1024;   // per-warp region
     constexpr int NB = SX > SY ? SX : SY;
     static_assert(YSTAGE % 128 == 0, "y output staging must stay 128-byte aligned");
@@ -904,7 +983,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) ensemble_kernel(const __grid_co
 template <class T, int SX, int RY, int BWY, int SY, int NW> constexpr size_t ensemble_smem() {
     constexpr int CX = 32 / sizeof(T);
     constexpr size_t XB = (size_t)SX * 4 * 32 * CX * sizeof(T);
-    constexpr size_t YB = SY * (size_t)4 * RY * BWY * sizeof(T) + 2 * (size_t)4 * RY * 32 * sizeof(T);
+    constexpr size_t YB = SY * (size_t)4 * RY * BWY * sizeof(T) + 2 * (size_t)4 * kYLag * 32 * sizeof(T);
     constexpr size_t WB = ((XB > YB ? XB : YB) + 1023) / 1024 * 1024;
     constexpr int NB = SX > SY ? SX : SY;
     return 1024 + NW * WB + NW * NB * sizeof(uint64_t);

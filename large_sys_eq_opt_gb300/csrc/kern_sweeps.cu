@@ -99,9 +99,16 @@ static cudaError_t LAUNCH_F(const void* in, const void* out, int nx, int ny, dou
 }
 
 constexpr size_t kSmemE = ensemble_smem<T, SX, RY, BWY, SY, NW>();
+// The persistent ensemble kernel holds both sweeps' code: FP32 at 3 CTAs per
+// SM (<= 168 registers; at 128 it spilled 188 bytes, 64-instance ensemble
+// 27.5 -> 26.4 ms per 50 steps), FP64 as its y-sweep.
+#ifndef EU_MINB_E
+#define EU_MINB_E (EU_PREC == 32 ? 3 : 2)
+#endif
+constexpr int MINB_E = EU_MINB_E;
 
 static cudaError_t LAUNCH_E(const void* args, int ctas, cudaStream_t s) {
-    auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_Y>;
+    auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_E>;
     static PerDevice<cudaError_t> attr_cache;
     const cudaError_t attr = attr_cache.get(
         [k] { return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemE); });
@@ -111,7 +118,7 @@ static cudaError_t LAUNCH_E(const void* args, int ctas, cudaStream_t s) {
 }
 
 static int OCC_E() {
-    auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_Y>;
+    auto k = ensemble_kernel<T, SOL, SX, RY, BWY, SY, NW, MINB_E>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemE);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, kSmemE) != cudaSuccess) return 1;

@@ -288,8 +288,9 @@ void eu_host_free(void* p);
  * passes the solver to every advance_second_order call,
  * head/cpu/solver_cpu.hpp:62-80, so one handle serves every solver of a
  * geometry; the state is kept, the launch plan becomes the planner's for the
- * new solver; an adjoint backward pass uses the solver of its forward pass,
- * and a batch's own ensemble steps keep the batch's solver).
+ * new solver; a completed adjoint forward pass is discarded, so
+ * eu_adjoint_backward returns EU_ERR_STATE until the next forward, and a
+ * batch's own ensemble steps keep the batch's solver).
  * Read-only: "tasks_x", "tasks_y".  Used by the tile-shape autotuner. */
 int eu_set_option(eu_handle* h, const char* name, long long value);
 int eu_get_option(eu_handle* h, const char* name, long long* value);

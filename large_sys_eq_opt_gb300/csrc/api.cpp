@@ -657,6 +657,7 @@ int eu_set_option(eu_handle* h, const char* name, long long value) {
             }
             h->solver = (int)value;
             h->K = kernels_for(h->prec, h->solver);
+            h->adj.ready = false;   // a completed adjoint forward belongs to the old solver
             // the solvers' y-sweeps load boxes of different heights (8 or 4
             // rows): re-encode the maps that carry the box
             if (h->K.ry != h->tm_y_ry)

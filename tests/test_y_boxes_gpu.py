@@ -105,3 +105,20 @@ def test_solver_switch_reencodes_the_y_boxes(E):
         r.upload(U0)
         r.adjoint_forward(dts, ckpt_k=2)
         assert np.array_equal(got_adj, r.download())
+
+
+def test_solver_switch_discards_the_adjoint_forward(E):
+    """A backward pass after a solver switch would linearise another
+    solver's steps: it is refused until the next forward pass."""
+    prob = problems()[0]
+    dts = [2.0e-3, 1.5e-3]
+    with E.Solver.for_problem(prob, "fp32", "hllc") as s:
+        s.adjoint_forward(dts, ckpt_k=2)
+        seed = np.zeros_like(s.download())
+        seed[2:-2, 2:-2, 0] = 1.0
+        s.set_option("solver", 0)          # HLL
+        with pytest.raises(E.EulerError):
+            s.adjoint_backward(seed)
+        s.adjoint_forward(dts, ckpt_k=2)
+        g = s.adjoint_backward(seed)
+        assert np.all(np.isfinite(g))

@@ -42,6 +42,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# The ensemble gradient leg runs 64 grids on their own streams; 32 hardware
+# work queues instead of CUDA's default 8 let more of them run at once.  CUDA
+# reads this when the context is created, so it is set before any device use.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "cell-updates/s FP32 vs FP64 at stated L1 err vs FP64; adjoint/forward time ratio"
 UNIT = "cell-updates/s"
@@ -474,19 +478,28 @@ def ensemble_leg(E, np, steps=20):
         cells = b.cells
     # batched gradients of every instance w.r.t. its two scalar parameters,
     # device-resident (eu_batch_param_gradients); the first call also
-    # allocates the checkpoint workspace, the second is the timed one
+    # allocates the adjoint workspace, the second is the timed one.  ckpt_k 0
+    # keeps every step's state in HBM when it fits (no recomputation); the
+    # same call with checkpoints every 32 steps is timed beside it.
     from large_sys_eq_opt_gb300 import adjoint as A
     nadj = 100
     with E.Batch(probs, "fp32", "hllc") as b:
         b.autotune(2)
         t0 = time.perf_counter()
         A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b)
+        A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b)
+        t_k32 = time.perf_counter()
+        A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b)
+        t_k32 = time.perf_counter() - t_k32
+        t0 = time.perf_counter()
+        A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 0, batch=b)
         t_first = time.perf_counter() - t0
         t0 = time.perf_counter()
         parts = {}
-        Js, grads, dts, _ = A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 32, batch=b,
+        Js, grads, dts, _ = A.ensemble_parameter_gradients(E, probs, nadj, "fp32", "hllc", 0, batch=b,
                                                            timing=parts)
         t_all = time.perf_counter() - t0
+        ckpt_k = max(inst.get_option("ckpt_k") for inst in b.instances)
         fwd_ms = max(inst.adjoint_timing()[0] for inst in b.instances)
         bwd_ms = max(inst.adjoint_timing()[1] for inst in b.instances)
         for inst, p in zip(b.instances, probs):
@@ -498,12 +511,14 @@ def ensemble_leg(E, np, steps=20):
         b.start()
         plain_ms = b.time_steps(nadj)
     adj = {"steps": nadj, "params": "blast R (ramped interface) and p_in; bubble rho and Mach",
-           "path": "device-resident: eu_init_params, CFL ensemble run for the dt lists, "
-                   "eu_batch_param_gradients (checkpointed forwards, objective and dJ/dU_N, backward sweeps, "
-                   "tangent contractions on the device; 3 numbers per instance to the host)",
+           "path": "device-resident: eu_batch_param_gradients (initial states, checkpointed CFL forwards "
+                   "logging their dts, objective and dJ/dU_N, backward sweeps with those dts, tangent "
+                   "contractions on the device; 3 numbers per instance to the host)",
+           "ckpt_k": ckpt_k, "ckpt_rule": "0 = every step's state resident when it fits in half the free HBM",
            "plain_ensemble_forward_ms": plain_ms, "gradients_wall_s_total": t_all,
            "gradients_wall_s_first_call": t_first, "gradients_over_plain_forward": t_all * 1e3 / plain_ms,
-           "wall_s_dt_run": parts.get("dt_run_s"), "wall_s_param_gradients_call": parts.get("gradients_s"),
+           "gradients_wall_s_ckpt_k32": t_k32, "gradients_over_plain_forward_ckpt_k32": t_k32 * 1e3 / plain_ms,
+           "wall_s_param_gradients_call": parts.get("gradients_s"),
            "checkpointed_forward_ms_max_instance": fwd_ms, "backward_device_ms_max_instance": bwd_ms,
            "example_gradients": grads[:2] + grads[48:50]}
     seq_ms = 0.0

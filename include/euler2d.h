@@ -180,6 +180,13 @@ int eu_totals_noalloc(const double* d_aos, int nx, int ny, double* d_out, void* 
  * eu_adjoint_forward runs the nsteps steps from the current state, keeping a
  * checkpoint every ckpt_k steps (plus the last segment's intermediate
  * states); the handle's state becomes U_N and its time advances by sum(dts).
+ * With dts NULL the steps take CFL step sizes as eu_step_n does (chosen on
+ * the device from each state) and the backward differentiates with those
+ * sizes held fixed; eu_adjoint_dts returns them.  ckpt_k in [0, 1024]; 0
+ * keeps every step's state on the device (nothing recomputed by the
+ * backward) when that fits in half the free device memory, else
+ * checkpoints every ceil(sqrt(nsteps)) steps (the batched calls decide
+ * this once for all instances).
  * eu_adjoint_backward takes dJ/dU_N and returns dJ/dU_0 (both host grids in
  * Grid2D AoS layout; ghost entries of the input are ignored, those of the
  * output are zero), recomputing each earlier segment's states from its
@@ -187,6 +194,9 @@ int eu_totals_noalloc(const double* d_aos, int nx, int ny, double* d_out, void* 
  * arithmetic is the handle's precision.  Needs nx, ny >= 2. */
 int eu_adjoint_forward(eu_handle* h, long long nsteps, const double* dts, int ckpt_k);
 int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0);
+/* The step sizes of the last eu_adjoint_forward (given or CFL-chosen):
+ * *nsteps = their number, the first min(cap, *nsteps) copied to dts. */
+int eu_adjoint_dts(eu_handle* h, double* dts, long long cap, long long* nsteps);
 /* Device time (CUDA events) of the last eu_adjoint_forward (ms[0], its steps
  * only) and eu_adjoint_backward (ms[1], recomputation + adjoint sweeps). */
 int eu_adjoint_timing(eu_handle* h, float ms[2]);
@@ -222,6 +232,8 @@ int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]);
 /* Batched discrete adjoint: eu_adjoint_forward / eu_adjoint_backward of
  * every instance (instance i: nsteps[i] steps with its own frozen dts[i]),
  * enqueued on the instances' own streams so that they run concurrently.
+ * With dts NULL (or dts[i] NULL) instance i takes CFL steps as in
+ * eu_batch_step: at most nsteps[i], stopping at its own t_end.
  * Gradients with respect to scalar case parameters follow by the chain
  * rule dJ/dtheta = <dJ/dU_0, dU_0/dtheta> (large_sys_eq_opt_gb300/adjoint.py). */
 int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k);
@@ -244,7 +256,10 @@ int eu_init_params(eu_handle* h, const eu_case_params* p);
 /* Objective values and gradients with respect to two scalar parameters per
  * instance, entirely on the device: each instance starts from
  * eu_init_params(params[i]), runs nsteps[i] steps with the frozen step
- * sizes dts[i] (checkpoints every ckpt_k), J_i = sum of rho^2 over the ring
+ * sizes dts[i] (checkpoints every ckpt_k; dts or dts[i] NULL: CFL steps as
+ * in eu_batch_step, at most nsteps[i] and up to the instance's t_end, their
+ * sizes then held fixed and readable by eu_adjoint_dts on the instance's
+ * handle), J_i = sum of rho^2 over the ring
  * 0.6 <= r <= 0.8 from the blast centre or 1.2 r_b <= d <= 1.6 r_b from the
  * bubble centre, and dJ_i/dtheta = <dJ/dU_0, dU_0/dtheta> with the closed-form
  * tangents of the initial state.  dJ[2i], dJ[2i+1] = dJ/dR, dJ/dp_in (blast)
@@ -291,7 +306,9 @@ void eu_host_free(void* p);
  * new solver; a completed adjoint forward pass is discarded, so
  * eu_adjoint_backward returns EU_ERR_STATE until the next forward, and a
  * batch's own ensemble steps keep the batch's solver).
- * Read-only: "tasks_x", "tasks_y".  Used by the tile-shape autotuner. */
+ * Read-only: "tasks_x", "tasks_y", "occ_x", "occ_y", "sm_count", and
+ * "ckpt_k" (the checkpoint spacing of the last adjoint forward).  Used by
+ * the tile-shape autotuner. */
 int eu_set_option(eu_handle* h, const char* name, long long value);
 int eu_get_option(eu_handle* h, const char* name, long long* value);
 /* Tile-shape autotuner (no reference counterpart): times candidate segment

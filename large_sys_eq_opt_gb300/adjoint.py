@@ -131,39 +131,31 @@ def objective_grad(U: np.ndarray, mask: np.ndarray) -> np.ndarray:
 PARAM_NAMES = {"blast": ("r", "p_in"), "shock_bubble": ("rho_bubble", "mach")}
 
 
-def ensemble_parameter_gradients(E, problems, nsteps: int, precision="fp32", solver="hllc", ckpt_k: int = 32,
+def ensemble_parameter_gradients(E, problems, nsteps: int, precision="fp32", solver="hllc", ckpt_k: int = 0,
                                  batch=None, device=True, timing: dict | None = None):
-    """J and dJ/dtheta of every instance after (at most) nsteps CFL steps.
+    """J and dJ/dtheta of every instance after (at most) nsteps CFL steps,
+    each instance stopping at its own t_end; the step sizes are then held
+    fixed.
 
-    The dt sequences come from one ensemble run of the initial states (each
-    instance stops at its own t_end); the adjoint forward and backward of all
-    instances then run concurrently.  device=True keeps everything on the
-    GPU (initial states, objective, dJ/dU_N and the tangent contractions;
-    eu_batch_param_gradients); device=False is the same computation with
-    the grids passing through host arrays and the formulas of this module.
-    Returns (J list, gradient dict list, dts list, batch); `timing`, when
-    given, receives the wall seconds of the dt run ("dt_run_s") and of the
-    gradient call ("gradients_s") on the device path."""
+    device=True keeps everything on the GPU (eu_batch_param_gradients):
+    initial states, the checkpointed forwards -- which take the CFL steps
+    themselves and log their sizes, the same steps as an ensemble run --,
+    objective, dJ/dU_N, backward sweeps and the tangent contractions, all
+    instances concurrently.  device=False is the same computation with the
+    dt lists from one ensemble run and the grids passing through host
+    arrays and the formulas of this module.  Returns (J list, gradient dict
+    list, dts list, batch); `timing`, when given, receives the wall seconds
+    of the gradient call ("gradients_s") on the device path."""
     own = batch is None
     b = batch if batch is not None else E.Batch(problems, precision, solver)
     try:
         if device:
             import time
-            t0 = time.perf_counter()
-            for inst, p in zip(b.instances, problems):
-                inst.init_params(p)
-                inst.set_dt_log(nsteps)
-            b.start()
-            b.step(nsteps)
-            dts = []
-            for inst in b.instances:
-                _, n, _ = inst.time()
-                dts.append(inst.dt_log(min(n, nsteps)))
             t1 = time.perf_counter()
-            J, dJ = b.param_gradients(problems, dts, ckpt_k)
+            J, dJ = b.param_gradients(problems, None, ckpt_k, nsteps=nsteps)
             if timing is not None:
-                timing["dt_run_s"] = t1 - t0
                 timing["gradients_s"] = time.perf_counter() - t1
+            dts = [inst.adjoint_dts() for inst in b.instances]
             kinds = ["blast" if isinstance(p.params, BlastParams) else "shock_bubble" for p in problems]
             grads = [dict(zip(PARAM_NAMES[k], map(float, g))) for k, g in zip(kinds, dJ)]
             return [float(x) for x in J], grads, dts, b

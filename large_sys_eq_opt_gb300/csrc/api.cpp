@@ -685,6 +685,7 @@ int eu_get_option(eu_handle* h, const char* name, long long* value) {
     else if (k == "occ_y") *value = h->K.occ_y();
     else if (k == "sm_count") *value = h->sm_count;
     else if (k == "tasks_y") *value = h->ntasks_y;
+    else if (k == "ckpt_k") *value = h->adj.k;
     else return fail(h, EU_ERR_INVALID, "unknown option " + k);
     return EU_OK;
 }

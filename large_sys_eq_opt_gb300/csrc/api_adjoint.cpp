@@ -62,11 +62,46 @@ int adj_alloc_buf(eu_handle* h, size_t bytes, void** p) {
     return EU_OK;
 }
 
+// Device bytes of the adjoint buffers for nsteps steps at spacing k
+// (adj_prepare), and of those the handle holds now.
+size_t adj_bytes(const eu_handle* h, long long nsteps, int k) {
+    const size_t nseg = (size_t)((nsteps + k - 1) / k);
+    return (nseg + 1 + (size_t)(k - 1) + 2) * state_bytes(h) + (size_t)k * tmp_bytes(h);
+}
+size_t adj_held_bytes(const eu_handle* h) {
+    const auto& A = h->adj;
+    if (A.ck.empty()) return 0;
+    return (A.ck.size() + A.R.size() - 1 + 2) * state_bytes(h) + A.Q.size() * tmp_bytes(h);
+}
+
+// Checkpoint spacing for ckpt_k = 0 over n handles: every step's state
+// resident (one segment each, nothing recomputed by the backward) when all
+// the handles' buffers fit in half of the device memory that is free or
+// already theirs, else ceil(sqrt(max nsteps)) (each segment recomputed once).
+// Handle i then uses min(k, nsteps[i]).
+int adj_auto_k(eu_handle* const* hs, const long long* nsteps, int n) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        (void)cudaGetLastError();
+        free_b = 0;
+    }
+    long long nmax = 1;
+    size_t need = 0, held = 0;
+    for (int i = 0; i < n; ++i) {
+        const long long s = std::max(1LL, nsteps[i]);
+        nmax = std::max(nmax, s);
+        need += adj_bytes(hs[i], s, (int)std::min<long long>(s, kMaxCkptK));
+        held += adj_held_bytes(hs[i]);
+    }
+    if (need <= (free_b + held) / 2) return (int)std::min<long long>(nmax, kMaxCkptK);
+    return (int)std::min<long long>(kMaxCkptK, (long long)std::ceil(std::sqrt((double)nmax)));
+}
+
 // Buffers for nsteps steps with checkpoints every k steps.
 int adj_prepare(eu_handle* h, long long nsteps, int k) {
     auto& A = h->adj;
     const int nseg = (int)((nsteps + k - 1) / k);
-    if (A.k != k || A.nseg < nseg) {
+    if (A.k != k || (int)A.ck.size() < nseg + 1) {
         EU_CUDA(h, cudaStreamSynchronize(h->st));
         adj_free(h);
         A.ck.assign(nseg + 1, nullptr);
@@ -119,13 +154,10 @@ int adj_prepare(eu_handle* h, long long nsteps, int k) {
     return EU_OK;
 }
 
-// Forward steps s*k .. s*k+len-1 from ck[s] with the frozen dts: the x-sweep
-// of step j writes Q[j], the y-sweep writes R[j+1] (ck[s+1] for the last).
-template <class T> cudaError_t adj_segment_t(eu_handle* h, int s) {
+// Control block of a frozen-dt forward from step s*k (pinned image hctl[s]).
+cudaError_t adj_push_frozen(eu_handle* h, int s) {
     auto& A = h->adj;
-    if (A.q_y_ry != h->K.ry) return cudaErrorInvalidValue;   // see launch_y
     const long long n0 = (long long)s * A.k;
-    const int len = (int)std::min<long long>(A.k, A.nsteps - n0);
     Ctl& c = A.hctl[s];
     std::memset(&c, 0, sizeof(Ctl));
     c.t_end = INFINITY;
@@ -137,7 +169,21 @@ template <class T> cudaError_t adj_segment_t(eu_handle* h, int s) {
     c.step = n0;
     c.dt = A.dts[n0];
     c.max_steps = LLONG_MAX;
-    cudaError_t e = cudaMemcpyAsync(h->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, h->st);
+    return cudaMemcpyAsync(h->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, h->st);
+}
+
+// Forward steps s*k .. s*k+len-1 from ck[s]: the x-sweep of step j writes
+// Q[j], the y-sweep writes R[j+1] (ck[s+1] for the last).  With `frozen`
+// the segment starts a control block that steps with the dt list d_dts;
+// otherwise it continues the control block on the device (the CFL forward,
+// whose y-sweeps choose and log each next dt).
+template <class T> cudaError_t adj_segment_t(eu_handle* h, int s, bool frozen) {
+    auto& A = h->adj;
+    if (A.q_y_ry != h->K.ry) return cudaErrorInvalidValue;   // see launch_y
+    const long long n0 = (long long)s * A.k;
+    const int len = (int)std::min<long long>(A.k, A.nsteps - n0);
+    cudaError_t e = cudaSuccess;
+    if (frozen) e = adj_push_frozen(h, s);
     for (int j = 0; j < len && e == cudaSuccess; ++j) {
         SweepArgs<T> ax = x_args<T>(h, 0);
         ax.out = Planes<T>{static_cast<T*>(A.Q[j]), h->pitch_t, h->plane_t};
@@ -154,77 +200,179 @@ template <class T> cudaError_t adj_segment_t(eu_handle* h, int s) {
     }
     return e;
 }
-cudaError_t adj_segment(eu_handle* h, int s) {
-    return h->prec == EU_FP32 ? adj_segment_t<float>(h, s) : adj_segment_t<double>(h, s);
+cudaError_t adj_segment(eu_handle* h, int s, bool frozen = true) {
+    return h->prec == EU_FP32 ? adj_segment_t<float>(h, s, frozen) : adj_segment_t<double>(h, s, frozen);
 }
 
-// Adjoint of step n = s*k + j (the ring holds segment s): y-sweep adjoint
-// lam -> mu on the x-sweep output Q[j], then x-sweep adjoint mu -> lam on the
-// step's input state.
-cudaError_t adj_step(eu_handle* h, int s, int j) {
-    auto& A = h->adj;
+// Arguments of the adjoint sweeps of step n = s*k + j (the ring holds
+// segment s): dir 1, the y-sweep adjoint lam -> mu on the x-sweep output
+// Q[j]; dir 0, the x-sweep adjoint mu -> lam on the step's input state.
+AdjSweepArgs adj_step_args(const eu_handle* h, int s, int j, int dir) {
+    const auto& A = h->adj;
     const long long n = (long long)s * A.k + j;
-    const AdjLaunch L = adj_launcher(h->prec, h->solver);
-    AdjSweepArgs y{};
-    y.P = A.Q[j]; y.p_pitch = h->pitch_t; y.p_plane = h->plane_t; y.p_coff = kTOff;
-    y.A = A.lam; y.a_pitch = h->pitch_s; y.a_plane = h->plane_s; y.a_coff = kSOff;
-    y.G = A.mu; y.g_pitch = h->pitch_s; y.g_plane = h->plane_s; y.g_coff = kSOff;
-    y.nx = h->cfg.nx; y.ny = h->cfg.ny;
-    y.lam_d = A.dts[n] / h->dy;
-    y.bc_lo = h->bc[EU_SIDE_BOTTOM]; y.bc_hi = h->bc[EU_SIDE_TOP];
-    cudaError_t e = L(1, y, h->st);
-    if (e != cudaSuccess) return e;
-    AdjSweepArgs x{};
-    x.P = j == 0 ? A.ck[s] : A.R[j]; x.p_pitch = h->pitch_s; x.p_plane = h->plane_s; x.p_coff = kSOff;
-    x.A = A.mu; x.a_pitch = h->pitch_s; x.a_plane = h->plane_s; x.a_coff = kSOff;
-    x.G = A.lam; x.g_pitch = h->pitch_s; x.g_plane = h->plane_s; x.g_coff = kSOff;
-    x.nx = h->cfg.nx; x.ny = h->cfg.ny;
-    x.lam_d = A.dts[n] / h->dx;
-    x.bc_lo = h->bc[EU_SIDE_LEFT]; x.bc_hi = h->bc[EU_SIDE_RIGHT];
-    return L(0, x, h->st);
+    AdjSweepArgs a{};
+    if (dir == 1) {
+        a.P = A.Q[j]; a.p_pitch = h->pitch_t; a.p_plane = h->plane_t; a.p_coff = kTOff;
+        a.A = A.lam; a.G = A.mu;
+        a.lam_d = A.dts[n] / h->dy;
+        a.bc_lo = h->bc[EU_SIDE_BOTTOM]; a.bc_hi = h->bc[EU_SIDE_TOP];
+    } else {
+        a.P = j == 0 ? A.ck[s] : A.R[j]; a.p_pitch = h->pitch_s; a.p_plane = h->plane_s; a.p_coff = kSOff;
+        a.A = A.mu; a.G = A.lam;
+        a.lam_d = A.dts[n] / h->dx;
+        a.bc_lo = h->bc[EU_SIDE_LEFT]; a.bc_hi = h->bc[EU_SIDE_RIGHT];
+    }
+    a.a_pitch = h->pitch_s; a.a_plane = h->plane_s; a.a_coff = kSOff;
+    a.g_pitch = h->pitch_s; a.g_plane = h->plane_s; a.g_coff = kSOff;
+    a.nx = h->cfg.nx; a.ny = h->cfg.ny;
+    return a;
 }
 
-// Enqueue the checkpointed forward on the handle's stream (no host wait).
-int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
+cudaError_t adj_step(eu_handle* h, int s, int j) {
+    const AdjLaunch L = adj_launcher(h->prec, h->solver);
+    cudaError_t e = L(1, adj_step_args(h, s, j, 1), h->st);
+    if (e != cudaSuccess) return e;
+    return L(0, adj_step_args(h, s, j, 0), h->st);
+}
+
+// The ensemble kernel's view of forward step n of the handle's checkpointed
+// forward (as adj_segment_t launches it): x-sweep from ck[s] or R[j] into
+// Q[j], y-sweep from Q[j] into R[j+1] (ck[s+1] for a segment's last step),
+// the same buffers whichever state buffer the control block names.
+template <class T> EnsInst<T> adj_ens_inst(const eu_handle* h, long long n) {
+    const auto& A = h->adj;
+    const int s = (int)(n / A.k), j = (int)(n % A.k);
+    const int len = (int)std::min<long long>(A.k, A.nsteps - (long long)s * A.k);
+    const bool last = j == len - 1;
+    EnsInst<T> I;
+    std::memset(&I, 0, sizeof(I));
+    I.tm_x[0] = I.tm_x[1] = j == 0 ? A.ck_x[s] : A.R_x[j];
+    I.tm_xo = A.Q_xo[j];
+    I.tm_y = A.Q_y[j];
+    I.tm_yo[0] = I.tm_yo[1] = last ? A.ck_yo[s + 1] : A.R_yo[j + 1];
+    I.xa = x_args<T>(h, 0);
+    I.xa.out = Planes<T>{static_cast<T*>(A.Q[j]), h->pitch_t, h->plane_t};
+    I.xa.snap = nullptr;
+    I.ya[0] = y_args<T>(h, 0);
+    I.ya[0].out = Planes<T>{static_cast<T*>(last ? A.ck[s + 1] : A.R[j + 1]), h->pitch_s, h->plane_s};
+    I.ya[0].out_index = 0;
+    I.ya[1] = I.ya[0];
+    return I;
+}
+template EnsInst<float> adj_ens_inst<float>(const eu_handle*, long long);
+template EnsInst<double> adj_ens_inst<double>(const eu_handle*, long long);
+
+// The checkpointed forward, in three parts so that an ensemble can run the
+// steps of all its instances in shared launches: adj_fwd_setup (buffers,
+// checkpoint 0 and the control block of the first step), the steps
+// (adj_segment per segment, or the ensemble kernel over adj_ens_inst
+// descriptors), adj_fwd_done (timing event, control-block probe).  All on
+// the handle's stream; no host wait.
+// With a dt list the steps use it; without one (dts null) they take CFL
+// steps as eu_step_n does -- the first dt from the initial state, each next
+// one from the y-sweep's reduction, clipped to t_end -- and log them into
+// d_dts, so that the backward replays exactly the steps taken.  A CFL
+// forward stops early once t reaches t_end (adj_fwd_finish trims it).
+int adj_fwd_setup(eu_handle* h, long long nsteps, const double* dts, int ckpt_k, double t_end) {
     if (!h) return fail(nullptr, EU_ERR_INVALID, "null handle");
-    if (nsteps < 1 || !dts) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: need nsteps >= 1 and a dt list");
-    if (ckpt_k < 1 || ckpt_k > 1024) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: ckpt_k must be in [1, 1024]");
+    if (nsteps < 1) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: need nsteps >= 1");
+    if (ckpt_k < 0 || ckpt_k > kMaxCkptK) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: ckpt_k must be in [0, 1024]");
     if (h->cfg.nx < 2 || h->cfg.ny < 2) return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: the adjoint needs nx, ny >= 2");
-    for (long long i = 0; i < nsteps; ++i)
-        if (!(dts[i] > 0.0) || !(dts[i] < INFINITY))
-            return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: every dt must be positive and finite");
+    if (dts)
+        for (long long i = 0; i < nsteps; ++i)
+            if (!(dts[i] > 0.0) || !(dts[i] < INFINITY))
+                return fail(h, EU_ERR_INVALID, "eu_adjoint_forward: every dt must be positive and finite");
+    if (ckpt_k == 0) ckpt_k = (int)std::min<long long>(adj_auto_k(&h, &nsteps, 1), nsteps);
     auto& A = h->adj;
     A.ready = false;
     if (int rc = adj_prepare(h, nsteps, ckpt_k)) return rc;
-    A.dts.assign(dts, dts + nsteps);
+    A.cfl = dts == nullptr;
     A.t0 = h->hctl->t;
     A.step0 = h->hctl->step;
-    EU_CUDA(h, cudaMemcpyAsync(A.d_dts, A.dts.data(), sizeof(double) * (size_t)nsteps, cudaMemcpyHostToDevice, h->st));
+    if (A.cfl) {
+        A.dts.clear();
+    } else {
+        A.dts.assign(dts, dts + nsteps);
+        EU_CUDA(h, cudaMemcpyAsync(A.d_dts, A.dts.data(), sizeof(double) * (size_t)nsteps, cudaMemcpyHostToDevice, h->st));
+    }
     EU_CUDA(h, fill_ghosts(h, h->cur));   // scripts/cpu/main_cpu.cpp:222
     EU_CUDA(h, cudaMemcpyAsync(A.ck[0], h->S[h->cur], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
     EU_CUDA(h, cudaEventRecord(A.ev[0], h->st));
-    for (int s = 0; s < A.nseg; ++s) EU_CUDA(h, adj_segment(h, s));
+    if (A.cfl) {
+        Ctl& c = A.hctl[0];
+        std::memset(&c, 0, sizeof(Ctl));
+        c.t = A.t0;
+        c.t_end = t_end;
+        c.cfl_dmin = h->cfg.cfl * std::min(h->dx, h->dy);
+        c.mode = kModeCfl;
+        c.max_steps = nsteps;
+        c.dt_log = A.d_dts;
+        c.dt_log_cap = nsteps;
+        EU_CUDA(h, cudaMemcpyAsync(h->ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, h->st));
+        EU_CUDA(h, launch_dt(h, h->cur));   // scripts/cpu/main_cpu.cpp:224
+    } else {
+        EU_CUDA(h, adj_push_frozen(h, 0));
+    }
+    return EU_OK;
+}
+
+int adj_fwd_done(eu_handle* h) {
+    auto& A = h->adj;
     EU_CUDA(h, cudaEventRecord(A.ev[1], h->st));
     A.ring_seg = A.nseg - 1;
-    EU_CUDA(h, cudaMemcpyAsync(h->S[h->cur], A.ck[A.nseg], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
     EU_CUDA(h, cudaMemcpyAsync(&A.hctl[A.nseg], h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
     return EU_OK;
 }
 
-// Wait for the forward; status, timing, the handle's time and step.
+int adj_fwd_steps(eu_handle* h) {
+    auto& A = h->adj;
+    // segment 0's control block comes from adj_fwd_setup; a frozen forward
+    // restarts it at each later segment, a CFL forward carries it on
+    for (int s = 0; s < A.nseg; ++s) EU_CUDA(h, adj_segment(h, s, !A.cfl && s > 0));
+    return adj_fwd_done(h);
+}
+
+int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k, double t_end) {
+    if (int rc = adj_fwd_setup(h, nsteps, dts, ckpt_k, t_end)) return rc;
+    return adj_fwd_steps(h);
+}
+
+// Wait for the forward; status, timing, the dt list of a CFL forward (and
+// its length, when it reached t_end early), the final state into the
+// handle's state buffer, the handle's time and step.
 int adj_fwd_finish(eu_handle* h) {
     auto& A = h->adj;
     EU_CUDA(h, cudaStreamSynchronize(h->st));
     EU_CUDA(h, cudaEventElapsedTime(&A.ms_fwd, A.ev[0], A.ev[1]));
     const Ctl probe = A.hctl[A.nseg];
+    if (probe.status & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
+    if (probe.status & kStatusNonFinite) return fail(h, EU_ERR_NONPHYSICAL, "non-finite state in the forward steps");
+    if (probe.status & kStatusNonPhysical)
+        return fail(h, EU_ERR_NONPHYSICAL, "compute_dt: non-positive maximum wave speed.");
+    void* fin = A.ck[A.nseg];
+    if (A.cfl) {
+        const long long n = probe.step;
+        if (n < 1 || n > A.nsteps) return fail(h, EU_ERR_STATE, "eu_adjoint_forward: no step before t_end");
+        A.dts.resize((size_t)n);
+        EU_CUDA(h, cudaMemcpyAsync(A.dts.data(), A.d_dts, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+        EU_CUDA(h, cudaStreamSynchronize(h->st));
+        if (n < A.nsteps) {
+            // the launches after step n found the control block done; the
+            // ring holds segment s up to its step j
+            const int s = (int)((n - 1) / A.k), j = (int)((n - 1) % A.k);
+            fin = j == A.k - 1 ? A.ck[s + 1] : A.R[j + 1];
+            A.nsteps = n;
+            A.nseg = s + 1;
+            A.ring_seg = s;
+        }
+    }
+    EU_CUDA(h, cudaMemcpyAsync(h->S[h->cur], fin, state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
     double t = A.t0;
-    for (double d : A.dts) t += d;
+    for (double d : A.dts) t += d;   // the device's own sum: t_new = t + dt per step
     ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
     h->hctl->t = t;
     h->hctl->step = A.step0 + A.nsteps;
     if (int rc = ctl_push(h)) return rc;
-    if (probe.status & kStatusTimeout) return fail(h, EU_ERR_TIMEOUT, "a bounded device wait expired");
-    if (probe.status & kStatusNonFinite) return fail(h, EU_ERR_NONPHYSICAL, "non-finite state in the forward steps");
     A.ready = true;
     return EU_OK;
 }
@@ -290,8 +438,18 @@ extern "C" {
 // --- discrete adjoint -----------------------------------------------------------
 int eu_adjoint_forward(eu_handle* h, long long nsteps, const double* dts, int ckpt_k) {
     Range range_("eu_adjoint_forward");
-    if (int rc = adj_fwd_enqueue(h, nsteps, dts, ckpt_k)) return rc;
+    if (int rc = adj_fwd_enqueue(h, nsteps, dts, ckpt_k, INFINITY)) return rc;
     return adj_fwd_finish(h);
+}
+
+int eu_adjoint_dts(eu_handle* h, double* dts, long long cap, long long* nsteps) {
+    if (!h || !nsteps || (cap > 0 && !dts)) return fail(h, EU_ERR_INVALID, "eu_adjoint_dts: bad argument");
+    const auto& A = h->adj;
+    if (!A.ready) return fail(h, EU_ERR_STATE, "eu_adjoint_dts: call eu_adjoint_forward first");
+    *nsteps = (long long)A.dts.size();
+    const long long n = std::min<long long>(cap, *nsteps);
+    if (n > 0) std::memcpy(dts, A.dts.data(), sizeof(double) * (size_t)n);
+    return EU_OK;
 }
 
 int eu_adjoint_backward(eu_handle* h, const double* dJ_dUN, double* dJ_dU0) {

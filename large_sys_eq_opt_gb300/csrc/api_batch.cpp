@@ -103,6 +103,11 @@ int batch_pull(eu_batch* b, int* all_done) {
 
 using namespace eu::rt;
 
+namespace {
+bool batch_adj_shared(const eu_batch* b);
+int batch_adj_steps(eu_batch* b);
+}  // namespace
+
 extern "C" {
 
 // --- ensemble ------------------------------------------------------------------
@@ -151,6 +156,8 @@ void eu_batch_destroy(eu_batch* b) {
     for (eu_handle* h : b->h) eu_destroy(h);
     cudaFree(b->d_inst);
     cudaFree(b->d_sched);
+    cudaFree(b->d_adj);
+    if (b->adj_ev) cudaEventDestroy(b->adj_ev);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
 }
@@ -302,11 +309,21 @@ int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]) {
 // Adjoints of every instance, enqueued on the instances' own streams so that
 // they run concurrently, then awaited.
 int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k) {
-    if (!b || !nsteps || !dts) return bfail(b, EU_ERR_INVALID, "bad argument");
+    if (!b || !nsteps) return bfail(b, EU_ERR_INVALID, "bad argument");
     if (cudaStreamSynchronize(b->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "batch stream failed");
+    const int K = ckpt_k == 0 ? adj_auto_k(b->h.data(), nsteps, b->n) : ckpt_k;
     for (int i = 0; i < b->n; ++i)
-        if (int rc = adj_fwd_enqueue(b->h[(size_t)i], nsteps[i], dts[i], ckpt_k))
+        if (int rc = adj_fwd_setup(b->h[(size_t)i], nsteps[i], dts ? dts[i] : nullptr,
+                                   ckpt_k == 0 ? (int)std::min<long long>(K, std::max(1LL, nsteps[i])) : ckpt_k,
+                                   b->h[(size_t)i]->cfg.t_end))
             return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+    if (batch_adj_shared(b)) {
+        if (int rc = batch_adj_steps(b)) return rc;
+    } else {
+        for (int i = 0; i < b->n; ++i)
+            if (int rc = adj_fwd_steps(b->h[(size_t)i]))
+                return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
+    }
     for (int i = 0; i < b->n; ++i)
         if (int rc = adj_fwd_finish(b->h[(size_t)i]))
             return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
@@ -404,6 +421,86 @@ template <class F> int for_instances(int n, int threads, F f) {
     return rc.load();
 }
 
+#define B_CUDA(call)                                                                              \
+    do {                                                                                          \
+        const cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return bfail(b, EU_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Device scratch of the batch's shared adjoint launches (grown, not shrunk).
+int batch_adj_scratch(eu_batch* b, size_t bytes) {
+    if (!b->adj_ev) B_CUDA(cudaEventCreateWithFlags(&b->adj_ev, cudaEventDisableTiming));
+    if (bytes <= b->adj_cap) return EU_OK;
+    B_CUDA(cudaStreamSynchronize(b->st));
+    cudaFree(b->d_adj);
+    b->d_adj = nullptr;
+    b->adj_cap = 0;
+    B_CUDA(cudaMalloc(&b->d_adj, bytes));
+    b->adj_cap = bytes;
+    return EU_OK;
+}
+
+// Whether the instances' adjoint steps can share launches: every instance
+// on the batch's solver, with its y boxes (and its adjoint ring's) of the
+// batch kernel's height.
+bool batch_adj_shared(const eu_batch* b) {
+    for (const eu_handle* h : b->h)
+        if (h->solver != b->solver || h->tm_y_ry != b->K.ry || h->adj.q_y_ry != b->K.ry) return false;
+    return b->ctas > 0;
+}
+
+// The forward steps of every instance's checkpointed forward (each set up by
+// adj_fwd_setup on its own stream), as one ensemble launch per step on the
+// batch stream: step s of instance i runs from the descriptors of its ring
+// (adj_ens_inst), the ensemble kernel computing each tile as the single-grid
+// kernels do.  An instance with fewer steps sits out the later launches
+// (its control block is done), as in eu_batch_step.
+template <class T> int batch_adj_steps_t(eu_batch* b) {
+    const int n = b->n;
+    long long nmax = 0;
+    for (eu_handle* h : b->h) nmax = std::max(nmax, h->adj.nsteps);
+    const size_t bytes = sizeof(EnsInst<T>) * (size_t)nmax * (size_t)n;
+    if (int rc = batch_adj_scratch(b, bytes)) return rc;
+    for (eu_handle* h : b->h) {
+        B_CUDA(cudaEventRecord(h->adj.ev[4], h->st));
+        B_CUDA(cudaStreamWaitEvent(b->st, h->adj.ev[4], 0));
+    }
+    std::vector<EnsInst<T>> tab((size_t)nmax * (size_t)n);
+    EnsArgs<T> E;
+    std::memset(&E, 0, sizeof(E));
+    E.sched = b->d_sched;
+    E.ninst = n;
+    int tx = 0, ty = 0;
+    for (int i = 0; i < n; ++i) {
+        const eu_handle* h = b->h[(size_t)i];
+        E.x_off[i] = tx;
+        E.y_off[i] = ty;
+        tx += h->ntasks_x;
+        ty += h->ntasks_y;
+        for (long long st = 0; st < nmax; ++st)
+            tab[(size_t)st * n + i] = adj_ens_inst<T>(h, std::min(st, h->adj.nsteps - 1));
+    }
+    E.x_off[n] = tx;
+    E.y_off[n] = ty;
+    E.total_x = tx;
+    E.total_y = ty;
+    B_CUDA(cudaMemcpyAsync(b->d_adj, tab.data(), bytes, cudaMemcpyHostToDevice, b->st));
+    for (long long st = 0; st < nmax; ++st) {
+        E.inst = static_cast<const EnsInst<T>*>(b->d_adj) + (size_t)st * n;
+        B_CUDA(cudaMemsetAsync(b->d_sched, 0, sizeof(EnsSched), b->st));
+        B_CUDA(b->K.ens(&E, b->ctas, b->st));
+    }
+    B_CUDA(cudaEventRecord(b->adj_ev, b->st));
+    for (eu_handle* h : b->h) {
+        B_CUDA(cudaStreamWaitEvent(h->st, b->adj_ev, 0));
+        if (int rc = adj_fwd_done(h)) return rc;
+    }
+    return EU_OK;
+}
+int batch_adj_steps(eu_batch* b) {
+    return b->prec == EU_FP32 ? batch_adj_steps_t<float>(b) : batch_adj_steps_t<double>(b);
+}
+
 }  // namespace
 
 extern "C" {
@@ -422,7 +519,7 @@ int eu_init_params(eu_handle* h, const eu_case_params* p) {
 int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const long long* nsteps,
                              const double* const* dts, int ckpt_k, double* J, double* dJ) {
     Range range_("eu_batch_param_gradients");
-    if (!b || !params || !nsteps || !dts || !J || !dJ) return bfail(b, EU_ERR_INVALID, "bad argument");
+    if (!b || !params || !nsteps || !J || !dJ) return bfail(b, EU_ERR_INVALID, "bad argument");
     for (int i = 0; i < b->n; ++i)
         if (params[i].kind != 0 && params[i].kind != 1) return bfail(b, EU_ERR_INVALID, "bad parameter kind");
     if (cudaStreamSynchronize(b->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "batch stream failed");
@@ -437,7 +534,8 @@ int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const lo
     for (int i = 0; i < b->n; ++i) ps.push_back(param_state(b->h[(size_t)i], params[i]));
     const unsigned hw = std::thread::hardware_concurrency();
     const int threads = (int)std::max(1u, std::min(8u, hw ? hw : 1u));
-    // 1. every instance's initial state and checkpointed forward, enqueued
+    const int K = ckpt_k == 0 ? adj_auto_k(b->h.data(), nsteps, b->n) : ckpt_k;
+    // 1. every instance's initial state and forward set-up, enqueued
     int rc = for_instances(b->n, threads, [&](int i) {
         eu_handle* h = b->h[(size_t)i];
         ctl_reset(h, kModeHost, INFINITY, LLONG_MAX);
@@ -445,9 +543,24 @@ int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const lo
         drop_graphs(h);
         const cudaError_t e = h->prec == EU_FP32 ? init_params_t<float>(h, ps[(size_t)i]) : init_params_t<double>(h, ps[(size_t)i]);
         if (e != cudaSuccess) return cuda_fail(h, e, "parameter initial state");
-        return adj_fwd_enqueue(h, nsteps[i], dts[i], ckpt_k);
+        const int k = ckpt_k == 0 ? (int)std::min<long long>(K, std::max(1LL, nsteps[i])) : ckpt_k;
+        return adj_fwd_setup(h, nsteps[i], dts ? dts[i] : nullptr, k, h->cfg.t_end);
     });
-    // 2. as each forward completes: objective, backward sweeps, contraction
+    // 2. the forward steps: one ensemble launch per step when the instances
+    //    can share launches, else each instance's own segment launches
+    bool batch_err = false;
+    if (rc == EU_OK) {
+        if (batch_adj_shared(b)) {
+            rc = batch_adj_steps(b);
+            batch_err = rc != EU_OK;
+        } else {
+            rc = for_instances(b->n, threads, [&](int i) { return adj_fwd_steps(b->h[(size_t)i]); });
+        }
+    }
+    // 3. as each forward completes: objective, dJ/dU_N, backward sweeps and
+    //    tangent contraction on the instance's own stream (the adjoint
+    //    sweeps of many grids run faster as concurrent per-grid launches
+    //    than as shared launches over all of them)
     if (rc == EU_OK)
         rc = for_instances(b->n, threads, [&](int i) {
             eu_handle* h = b->h[(size_t)i];
@@ -459,6 +572,10 @@ int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const lo
                                        h->st));
             return (int)EU_OK;
         });
+    if (cudaStreamSynchronize(b->st) != cudaSuccess && rc == EU_OK) {
+        rc = bfail(b, EU_ERR_CUDA, std::string("batch stream: ") + cudaGetErrorString(cudaGetLastError()));
+        batch_err = true;
+    }
     for (int i = 0; i < b->n; ++i) {
         eu_handle* h = b->h[(size_t)i];
         if (cudaStreamSynchronize(h->st) != cudaSuccess && rc == EU_OK) rc = cuda_fail(h, cudaGetLastError(), "sync");
@@ -473,6 +590,7 @@ int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const lo
     cudaFree(d_res);
     cudaFreeHost(h_res);
     if (rc != EU_OK) {
+        if (batch_err) return rc;
         for (int i = 0; i < b->n; ++i)
             if (!b->h[(size_t)i]->err.empty()) return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->h[(size_t)i]->err);
         return bfail(b, rc, "eu_batch_param_gradients failed");

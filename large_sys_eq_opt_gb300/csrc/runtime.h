@@ -97,9 +97,10 @@ struct eu_handle {
         int hctl_cap = 0;
         int ring_seg = -1;
         bool ready = false;
+        bool cfl = false;            // forward chose its dts (CFL, logged into d_dts)
         double t0 = 0.0;
         long long step0 = 0;
-        cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+        cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // 4: cross-stream hand-off
         float ms_fwd = 0.f, ms_bwd = 0.f;
     } adj;
     std::string err;
@@ -119,6 +120,9 @@ struct eu_batch {
     cudaGraphExec_t g = nullptr;
     int gsteps = 0;
     int wait_extra = 0;
+    void* d_adj = nullptr;       // descriptors of the shared adjoint launches
+    size_t adj_cap = 0;
+    cudaEvent_t adj_ev = nullptr;
     std::string err;
 };
 
@@ -221,7 +225,13 @@ int download_from_state(eu_handle* h, int b, double* aos);
 
 // Discrete adjoint (api_adjoint.cpp).
 void adj_free(eu_handle* h);
-int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k);
+constexpr int kMaxCkptK = 1024;
+template <class T> EnsInst<T> adj_ens_inst(const eu_handle* h, long long n);
+int adj_fwd_setup(eu_handle* h, long long nsteps, const double* dts, int ckpt_k, double t_end);
+int adj_fwd_done(eu_handle* h);
+int adj_fwd_steps(eu_handle* h);
+int adj_auto_k(eu_handle* const* hs, const long long* nsteps, int n);
+int adj_fwd_enqueue(eu_handle* h, long long nsteps, const double* dts, int ckpt_k, double t_end);
 int adj_fwd_finish(eu_handle* h);
 int adj_bwd_enqueue(eu_handle* h, const double* dJ_dUN, double* dJ_dU0);
 int adj_bwd_sweeps(eu_handle* h);

@@ -75,7 +75,7 @@ EXPORTS = (
     "eu_batch_adjoint_forward", "eu_batch_adjoint_backward", "eu_batch_set_wait_extra", "eu_write_planes",
     "eu_save_state", "eu_load_state", "eu_domain_plan", "eu_domain_create", "eu_domain_destroy",
     "eu_domain_last_error", "eu_domain_upload_aos", "eu_domain_download_aos", "eu_domain_step_n",
-    "eu_domain_get_time", "eu_init_params", "eu_batch_param_gradients",
+    "eu_domain_get_time", "eu_init_params", "eu_batch_param_gradients", "eu_adjoint_dts",
 )
 
 _lib = None
@@ -138,6 +138,7 @@ def load(path: str = LIB_PATH):
     L.eu_adjoint_forward.argtypes = [H, C.c_longlong, _dp, C.c_int]
     L.eu_adjoint_backward.argtypes = [H, _dp, _dp]
     L.eu_adjoint_timing.argtypes = [H, C.POINTER(C.c_float)]
+    L.eu_adjoint_dts.argtypes = [H, _dp, C.c_longlong, C.POINTER(C.c_longlong)]
     L.eu_autotune.argtypes = [H, C.c_int, C.POINTER(C.c_longlong)]
     B = C.c_void_p
     L.eu_batch_create.argtypes = [C.c_int, C.POINTER(EuCase), C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(B)]
@@ -417,11 +418,24 @@ class Solver:
         return out
 
     # -- discrete adjoint ----------------------------------------------------------
-    def adjoint_forward(self, dts, ckpt_k: int = 32):
+    def adjoint_forward(self, dts, ckpt_k: int = 32, nsteps: int | None = None):
         """Run len(dts) frozen-dt steps from the current state, keeping
-        checkpoints every ckpt_k steps for adjoint_backward."""
+        checkpoints every ckpt_k steps for adjoint_backward.  dts None:
+        nsteps CFL steps (sizes chosen on the device, then held fixed by the
+        backward; adjoint_dts() returns them)."""
+        if dts is None:
+            self._check(self._L.eu_adjoint_forward(self._h, int(nsteps), None, int(ckpt_k)))
+            return
         d = np.ascontiguousarray(dts, dtype=np.float64)
         self._check(self._L.eu_adjoint_forward(self._h, len(d), _p(d), int(ckpt_k)))
+
+    def adjoint_dts(self) -> np.ndarray:
+        """Step sizes of the last adjoint_forward (given or CFL-chosen)."""
+        n = C.c_longlong()
+        self._check(self._L.eu_adjoint_dts(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        self._check(self._L.eu_adjoint_dts(self._h, _p(out), n.value, C.byref(n)))
+        return out
 
     def adjoint_backward(self, dJ_dUN: np.ndarray) -> np.ndarray:
         """dJ/dU_0 for dJ/dU_N (both (ny+4, nx+4, 4) float64; ghosts zero)."""
@@ -590,24 +604,32 @@ class Batch:
         self._check(self._L.eu_batch_autotune(self._b, int(steps), out))
         return int(out[0]), int(out[1])
 
-    def adjoint_forward(self, dts_list, ckpt_k: int = 32):
-        """Checkpointed forward of every instance with its own frozen dts."""
+    def _dt_lists(self, dts_list, nsteps):
+        """(step counts, dt pointer array or None, kept arrays) of the
+        batched adjoint calls; dts_list None: nsteps CFL steps each."""
         n = len(self.instances)
+        if dts_list is None:
+            return (C.c_longlong * n)(*[int(nsteps)] * n), None, []
         arrs = [np.ascontiguousarray(d, dtype=np.float64) for d in dts_list]
-        ns = (C.c_longlong * n)(*[len(a) for a in arrs])
-        ptrs = (_dp * n)(*[_p(a) for a in arrs])
-        self._keep = arrs
+        return (C.c_longlong * n)(*[len(a) for a in arrs]), (_dp * n)(*[_p(a) for a in arrs]), arrs
+
+    def adjoint_forward(self, dts_list, ckpt_k: int = 0, nsteps: int | None = None):
+        """Checkpointed forward of every instance with its own frozen dts
+        (dts_list None: at most nsteps CFL steps each, up to its t_end).
+        ckpt_k 0: every state resident when the instances' buffers fit in
+        half the free device memory, else checkpoints every sqrt(nsteps)."""
+        ns, ptrs, self._keep = self._dt_lists(dts_list, nsteps)
         self._check(self._L.eu_batch_adjoint_forward(self._b, ns, ptrs, int(ckpt_k)))
 
-    def param_gradients(self, problems, dts_list, ckpt_k: int = 32):
+    def param_gradients(self, problems, dts_list, ckpt_k: int = 0, nsteps: int | None = None):
         """J and the gradients with respect to each instance's two scalar
-        parameters, all on the device (eu_batch_param_gradients).  Returns
+        parameters, all on the device (eu_batch_param_gradients).  dts_list
+        None: at most nsteps CFL steps per instance, up to its t_end, whose
+        sizes the instances' adjoint_dts() return afterwards.  Returns
         (J array of n, dJ array of n x 2)."""
         n = len(self.instances)
         params = (EuCaseParams * n)(*[case_params(p) for p in problems])
-        dts = [np.ascontiguousarray(d, dtype=np.float64) for d in dts_list]
-        ns = (C.c_longlong * n)(*[len(d) for d in dts])
-        pd = (_dp * n)(*[_p(d) for d in dts])
+        ns, pd, dts = self._dt_lists(dts_list, nsteps)
         J = np.zeros(n)
         dJ = np.zeros(2 * n)
         self._check(self._L.eu_batch_param_gradients(self._b, params, ns, pd, int(ckpt_k), _p(J), _p(dJ)))

@@ -253,6 +253,36 @@ def test_adjoint_forward_matches_step_n(E):
         assert n >= 21 and abs(t - float(np.sum(dts))) <= 1e-12
 
 
+@pytest.mark.parametrize("prec,solver", [("fp32", "hllc"), ("fp64", "hllc"), ("fp32", "exact")])
+def test_cfl_adjoint_forward_equals_frozen(E, prec, solver):
+    """eu_adjoint_forward without a dt list takes eu_step_n's CFL steps
+    (the same sizes and state, 19 steps over checkpoints of 4) and its
+    backward equals, bit for bit, the backward of a forward given those
+    sizes."""
+    cfg = geometry(96, 80)
+    rho, p = blast_fields(cfg)
+    U0 = grid_of(cfg, rho, p)
+    mask = ring(cfg)
+    with E.Solver(cfg, prec, solver) as s:
+        s.upload(U0)
+        s.set_dt_log(19)
+        s.step_n(19)
+        plain, plain_dts = s.download(), s.dt_log(19)
+        s.upload(U0)
+        s.adjoint_forward(None, 4, nsteps=19)
+        a = s.download()
+        dts = s.adjoint_dts()
+        g1 = s.adjoint_backward(dJ_dU(a, mask))
+        s.upload(U0)
+        s.adjoint_forward(dts, 4)
+        b = s.download()
+        g2 = s.adjoint_backward(dJ_dU(b, mask))
+    assert np.array_equal(dts, plain_dts)
+    assert np.array_equal(a, plain) and np.array_equal(b, plain)
+    assert np.array_equal(g1, g2)
+    assert np.any(g1 != 0)
+
+
 def test_adjoint_config_512(E):
     """The adjoint benchmark geometry: 512^2, HLLC + minmod, 400 frozen-dt
     steps, checkpoints every 32, 16 seeded Gaussian directions, central

@@ -118,10 +118,11 @@ def test_batched_parameter_gradients_match_fd(E):
 
 
 def test_device_parameter_gradients_equal_host_path(E):
-    """eu_batch_param_gradients (initial states, objective, dJ/dU_N and the
-    tangent contractions on the device) against the same computation with
-    the grids passing through host arrays (adjoint.py formulas), FP64: the
-    same J and gradients to rounding."""
+    """eu_batch_param_gradients (initial states, CFL forwards, objective,
+    dJ/dU_N and the tangent contractions on the device) against the same
+    computation with the dt lists from an ensemble run and the grids
+    passing through host arrays (adjoint.py formulas), FP64: the same dt
+    lists bit for bit, J and gradients to rounding."""
     from large_sys_eq_opt_gb300 import adjoint as A
     bub = (TRANSMISSIVE, TRANSMISSIVE, REFLECTIVE, REFLECTIVE)
     probs = [
@@ -139,3 +140,77 @@ def test_device_parameter_gradients_equal_host_path(E):
     for a, b in zip(gd, gh):
         for k in b:
             assert abs(a[k] - b[k]) <= 1e-9 * abs(b[k]) + 1e-12, (k, a[k], b[k])
+
+
+@pytest.mark.parametrize("prec,solver", [("fp32", "hllc"), ("fp64", "hllc"), ("fp32", "exact")])
+def test_param_gradients_cfl_forward_equals_dt_run(E, prec, solver):
+    """eu_batch_param_gradients without dt lists: each instance's forward
+    takes the ensemble run's CFL steps -- the first blast reaches its t_end
+    after 14 of the 30 steps (the oracle's count), partway through a
+    checkpoint segment of 4 and at the end of one of 7; k = 0 keeps all 30
+    states (one segment) -- and J and the gradients equal, bit for bit,
+    those of the call given the ensemble run's dt lists.  The forwards run
+    as shared ensemble launches; the backward reads every state from the
+    ring with k = 0 and recomputes earlier segments with each instance's own
+    launches with k = 4 and 7, with the same bits."""
+    from large_sys_eq_opt_gb300 import adjoint as A
+    bub = (TRANSMISSIVE, TRANSMISSIVE, REFLECTIVE, REFLECTIVE)
+    probs = [
+        Problem(CaseConfig(64, 64, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.05), "blast", BlastParams(r=0.37, p_in=12.0)),
+        Problem(CaseConfig(140, 55, 2, 0.0, 0.225, 0.0, 0.089, 0.8, 0.1), "shock_bubble",
+                ShockBubbleParams(mach=1.7, rho_bubble=0.4), bc=bub),
+        Problem(CaseConfig(96, 80, 2, 0.0, 2.0, 0.0, 2.0, 0.8, 0.25), "blast", BlastParams(r=0.3, p_in=5.0)),
+    ]
+    nsteps = 30
+    res = {}
+    with E.Batch(probs, prec, solver) as b:
+        for k in (4, 7, 0):
+            Jc, gc, dtc, _ = A.ensemble_parameter_gradients(E, probs, nsteps, prec, solver, ckpt_k=k, batch=b)
+            for inst, p in zip(b.instances, probs):
+                inst.init_params(p)
+                inst.set_dt_log(nsteps)
+            b.start()
+            b.step(nsteps)
+            dts = [inst.dt_log(min(inst.time()[1], nsteps)) for inst in b.instances]
+            J, dJ = b.param_gradients(probs, dts, k)
+            if k == 0:
+                assert [inst.get_option("ckpt_k") for inst in b.instances] == [len(dts[0]), nsteps, nsteps]
+            assert len(dts[0]) < nsteps, len(dts[0])
+            assert [len(d) for d in dts[1:]] == [nsteps, nsteps]
+            for a, d in zip(dtc, dts):
+                assert np.array_equal(a, d), k
+            assert np.array_equal(np.array(Jc), J), k
+            assert np.array_equal(np.array([list(g.values()) for g in gc]), dJ), k
+            assert np.all(np.isfinite(dJ))
+            res[k] = (J, dJ)
+    for k in (4, 7):
+        assert np.array_equal(res[k][0], res[0][0]), k
+        assert np.array_equal(res[k][1], res[0][1]), k
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_batch_adjoint_forward_matches_single_steps(E, prec):
+    """eu_batch_adjoint_forward (the instances' steps as shared ensemble
+    launches, checkpoints every 3 steps) lands every instance on the state,
+    time and step count of its own handle's eu_step_n with the same dts."""
+    probs = small_ensemble()[:5]
+    nsteps = [7, 11, 5, 9, 8]
+    dts = []
+    for p, n in zip(probs, nsteps):
+        with E.Solver.for_problem(p, prec, "hllc") as s:
+            s.set_dt_log(n)
+            s.step_n(n)
+            dts.append(s.dt_log(n))
+    with E.Batch(probs, prec, "hllc") as b:
+        U0 = [inst.download() for inst in b.instances]
+        b.adjoint_forward(dts, 3)
+        got = [inst.download() for inst in b.instances]
+        times = [inst.time() for inst in b.instances]
+    for p, u0, d, g, (t, n, _) in zip(probs, U0, dts, got, times):
+        with E.Solver.for_problem(p, prec, "hllc") as s:
+            s.upload(u0)
+            s.step_n(len(d), d)
+            ref = s.download()
+        assert np.array_equal(g, ref), p
+        assert n == len(d)
+        assert abs(t - float(np.sum(d))) <= 1e-12, p

@@ -230,8 +230,10 @@ int eu_batch_time_steps(eu_batch* b, int nsteps, float* ms);
  * restored afterwards. */
 int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]);
 /* Batched discrete adjoint: eu_adjoint_forward / eu_adjoint_backward of
- * every instance (instance i: nsteps[i] steps with its own frozen dts[i]),
- * enqueued on the instances' own streams so that they run concurrently.
+ * every instance (instance i: nsteps[i] steps with its own frozen dts[i]).
+ * The forward steps of all instances run as one ensemble launch per step
+ * (while every instance is on the batch's solver; else each on its own
+ * stream), the backwards concurrently on the instances' own streams.
  * With dts NULL (or dts[i] NULL) instance i takes CFL steps as in
  * eu_batch_step: at most nsteps[i], stopping at its own t_end.
  * Gradients with respect to scalar case parameters follow by the chain
@@ -264,8 +266,9 @@ int eu_init_params(eu_handle* h, const eu_case_params* p);
  * bubble centre, and dJ_i/dtheta = <dJ/dU_0, dU_0/dtheta> with the closed-form
  * tangents of the initial state.  dJ[2i], dJ[2i+1] = dJ/dR, dJ/dp_in (blast)
  * or dJ/drho_bubble, dJ/dMach (shock-bubble).  Only these 3n numbers cross
- * the host link.  Instances run concurrently on their streams, enqueued by
- * several host threads. */
+ * the host link.  The forwards run as in eu_batch_adjoint_forward, the
+ * rest of each instance's work on its own stream, enqueued by several host
+ * threads. */
 int eu_batch_param_gradients(eu_batch* b, const eu_case_params* params, const long long* nsteps,
                              const double* const* dts, int ckpt_k, double* J, double* dJ);
 /* Test hook of the failure-detection path (no reference counterpart): with

@@ -753,11 +753,19 @@ EUA_HD void riemann_vjp(const C4<T>& UL, const C4<T>& UR, const C4<T>& Fb, C4<T>
 #define EUA_SYNC() ((void)0)
 #endif
 
-template <class T, int NL, int TC> struct TileMem {
-    static constexpr int W_ = TC + 6;
+// Shared tile of NL lines x (TC + 6) cells, one array per quantity.  With
+// lines fastest (LF: consecutive threads on consecutive lines, same cell)
+// the line stride is padded to one element past a multiple of 128 bytes, so
+// that a quarter-warp's 16-byte accesses fall on distinct banks (FP32; FP64
+// elements of 32 bytes: two per 128 bytes at most).  Cells fastest needs no
+// padding: consecutive threads read consecutive elements.
+template <class T, int NL, int TC, bool LF = false> struct TileMem {
+    static constexpr int kQ = 128 / (int)sizeof(C4<T>);
+    static constexpr int W_ = LF ? (TC + 6 - 1 + kQ - 1) / kQ * kQ + 1 : TC + 6;
     W4<T> W[NL][W_];
     C4<T> A[NL][W_];
-    C4<T> LR[NL][W_][2];   // L*, R* (P1) -> Lbar*, Rbar* (P2) -> contributions m, c (P3)
+    C4<T> L[NL][W_];       // L* (P1) -> adjoint of L* (P2) -> contribution to the left neighbour (P3)
+    C4<T> R[NL][W_];       // R* (P1) -> adjoint of R* (P2) -> contribution to the cell itself (P3)
     W4<T> Xp[NL][W_];      // contribution to the right neighbour (P3)
 };
 
@@ -768,7 +776,7 @@ template <bool LF, int NL> EUA_HD void tile_split(int idx, int width, int& l, in
 }
 
 template <int S, class T, int NL, int TC, bool LF, class Acc>
-EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC>& m, int line0, int c0, int tl, int tid, int nthr) {
+EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC, LF>& m, int line0, int c0, int tl, int tid, int nthr) {
     const int n = acc.n;
     const T hl = acc.hl, lam = acc.lam;
     // P0
@@ -796,8 +804,8 @@ EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC>& m, int line0, int c
             const int cc = k + 1;
             Recon<T> o;
             recon_primal(m.W[l][cc - 1], m.W[l][cc], m.W[l][cc + 1], hl, o);
-            m.LR[l][cc][0] = o.L;
-            m.LR[l][cc][1] = o.R;
+            m.L[l][cc] = o.L;
+            m.R[l][cc] = o.R;
         }
     }
     EUA_SYNC();
@@ -810,9 +818,9 @@ EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC>& m, int line0, int c
             const int cc = k + 1;
             const C4<T> Fb = scale(sub(m.A[l][cc + 1], m.A[l][cc]), lam);
             C4<T> Lb, Rb;
-            riemann_vjp<S>(m.LR[l][cc][1], m.LR[l][cc + 1][0], Fb, Lb, Rb);
-            m.LR[l][cc][1] = Lb;       // adjoint of R* of the left cell
-            m.LR[l][cc + 1][0] = Rb;   // adjoint of L* of the right cell
+            riemann_vjp<S>(m.R[l][cc], m.L[l][cc + 1], Fb, Lb, Rb);
+            m.R[l][cc] = Lb;       // adjoint of R* of the left cell
+            m.L[l][cc + 1] = Rb;   // adjoint of L* of the right cell
         }
     }
     EUA_SYNC();
@@ -826,9 +834,9 @@ EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC>& m, int line0, int c
             Recon<T> o;
             recon_primal(m.W[l][cc - 1], m.W[l][cc], m.W[l][cc + 1], hl, o);
             W4<T> bm = zerow<T>(), bc = zerow<T>(), bp = zerow<T>();
-            recon_vjp(o, hl, m.LR[l][cc][0], m.LR[l][cc][1], bm, bc, bp);
-            m.LR[l][cc][0] = C4<T>{bm.r, bm.un, bm.ut, bm.p};
-            m.LR[l][cc][1] = C4<T>{bc.r, bc.un, bc.ut, bc.p};
+            recon_vjp(o, hl, m.L[l][cc], m.R[l][cc], bm, bc, bp);
+            m.L[l][cc] = C4<T>{bm.r, bm.un, bm.ut, bm.p};
+            m.R[l][cc] = C4<T>{bc.r, bc.un, bc.ut, bc.p};
             m.Xp[l][cc] = bp;
         }
     }
@@ -845,10 +853,10 @@ EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC>& m, int line0, int c
             const int c = c0 + k;
             // primitive adjoint gathered from the reconstructions of c-1, c, c+1
             auto wbar = [&](int q, bool left_ok, bool right_ok) {
-                W4<T> b = W4<T>{m.LR[l][q][1].r, m.LR[l][q][1].mn, m.LR[l][q][1].mt, m.LR[l][q][1].e};
+                W4<T> b = W4<T>{m.R[l][q].r, m.R[l][q].mn, m.R[l][q].mt, m.R[l][q].e};
                 if (left_ok) add(b, m.Xp[l][q - 1]);
                 if (right_ok) {
-                    const C4<T>& x = m.LR[l][q + 1][0];
+                    const C4<T>& x = m.L[l][q + 1];
                     add(b, W4<T>{x.r, x.mn, x.mt, x.e});
                 }
                 return b;
@@ -867,7 +875,7 @@ EUA_HD void adjoint_tile(const Acc& acc, TileMem<T, NL, TC>& m, int line0, int c
                 const int q1 = cc - c - 1, q2 = cc - c - 2;   // tile slots of ghosts -1, -2
                 const C4<T> g1 = ubar(q1, wbar(q1, false, true));
                 W4<T> b2 = zerow<T>();
-                { const C4<T>& x = m.LR[l][q2 + 1][0]; add(b2, W4<T>{x.r, x.mn, x.mt, x.e}); }
+                { const C4<T>& x = m.L[l][q2 + 1]; add(b2, W4<T>{x.r, x.mn, x.mt, x.e}); }
                 const C4<T> g2 = ubar(q2, b2);
                 if (!refl_lo) { add(G, g1); add(G, g2); }
                 else if (c == 0) add(G, C4<T>{g1.r, -g1.mn, g1.mt, g1.e});

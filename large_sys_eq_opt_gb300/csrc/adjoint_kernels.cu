@@ -82,7 +82,7 @@ template <int DIR> struct DevAcc {
 template <int DIR, int NL, int TC>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) adjoint_sweep_kernel(const DevAcc<DIR> acc) {
     extern __shared__ __align__(16) unsigned char smem[];
-    auto& m = *reinterpret_cast<adj::TileMem<T, NL, TC>*>(smem);
+    auto& m = *reinterpret_cast<adj::TileMem<T, NL, TC, DIR == 1>*>(smem);
     const int ntile = (acc.n + TC - 1) / TC;
     const int g = blockIdx.x / ntile, t = blockIdx.x - g * ntile;
     int c0, c1;
@@ -104,7 +104,7 @@ template <int DIR, int NL, int TC> cudaError_t launch(const AdjSweepArgs& a, cud
     acc.hl = T(0.5 * a.lam_d);
     acc.bc_lo = a.bc_lo;
     acc.bc_hi = a.bc_hi;
-    constexpr size_t smem = sizeof(adj::TileMem<T, NL, TC>);
+    constexpr size_t smem = sizeof(adj::TileMem<T, NL, TC, DIR == 1>);
     auto k = adjoint_sweep_kernel<DIR, NL, TC>;
     static PerDevice<cudaError_t> attr_cache;
     const cudaError_t attr = attr_cache.get(

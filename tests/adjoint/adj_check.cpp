@@ -354,13 +354,17 @@ static void adjoint_sweep2(int dir, const Grid2<double>& P, const Grid2<double>&
                            const int bc[4]) {
     Acc2 acc{dir == 0 ? P.nx : P.ny, dir == 0 ? bc[0] : bc[2], dir == 0 ? bc[1] : bc[3], dir == 0 ? P.ny : P.nx,
              dir, 0.5 * lam, lam, &P, &A, &G};
-    static TileMem<double, 2, TC> mem;
+    // the tile layouts of the GPU kernels: lines fastest (padded line
+    // stride) for the y-sweep adjoint, cells fastest for the x-sweep adjoint
+    static TileMem<double, 2, TC> mem_x;
+    static TileMem<double, 2, TC, true> mem_y;
     const int nt = (acc.n + TC - 1) / TC;
     for (int l0 = 0; l0 < acc.nlines; l0 += 2)
         for (int t = 0; t < nt; ++t) {
             int c0, c1;
             tile_range(acc.n, TC, t, c0, c1);
-            adjoint_tile<S, double, 2, TC, false>(acc, mem, l0, c0, c1 - c0, 0, 1);
+            if (dir == 1) adjoint_tile<S, double, 2, TC, true>(acc, mem_y, l0, c0, c1 - c0, 0, 1);
+            else adjoint_tile<S, double, 2, TC, false>(acc, mem_x, l0, c0, c1 - c0, 0, 1);
         }
 }
 

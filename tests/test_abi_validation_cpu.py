@@ -47,6 +47,9 @@ def test_null_handles_are_rejected(L):
     assert L.eu_step_n(None, 3, None) == 1
     assert L.eu_totals(None, None) == 1
     assert L.eu_adjoint_forward(None, 1, None, 4) == 1
+    n = C.c_longlong()
+    assert L.eu_adjoint_dts(None, None, 0, C.byref(n)) == 1
+    assert L.eu_batch_adjoint_forward(None, None, None, 0) == 1
     assert L.eu_batch_step(None, 1, None) == 1
     assert L.eu_batch_handle(None, 0) is None
     L.eu_destroy(None)          # no-op

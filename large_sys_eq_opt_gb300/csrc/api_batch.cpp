@@ -306,8 +306,10 @@ int eu_batch_autotune(eu_batch* b, int steps, long long chosen[2]) {
     return EU_OK;
 }
 
-// Adjoints of every instance, enqueued on the instances' own streams so that
-// they run concurrently, then awaited.
+// Checkpointed forwards of every instance: set up on the instances' own
+// streams, the steps as shared ensemble launches (or each instance's own
+// launches), then awaited.  The backwards (next) run on the instances' own
+// streams, concurrently.
 int eu_batch_adjoint_forward(eu_batch* b, const long long* nsteps, const double* const* dts, int ckpt_k) {
     if (!b || !nsteps) return bfail(b, EU_ERR_INVALID, "bad argument");
     if (cudaStreamSynchronize(b->st) != cudaSuccess) return bfail(b, EU_ERR_CUDA, "batch stream failed");

@@ -1,5 +1,5 @@
 // ref_gpu_harness.cu -- runs the reference's OWN CUDA kernels on this GPU
-// (BASELINE MEASUREMENT / TEST INFRASTRUCTURE: never part of the product).
+// (comparison timing and test infrastructure: never part of the product).
 //
 // The reference's GPU solver (src/gpu/solver_gpu.cu) is compiled, unmodified,
 // from its own sources into a device image (oracle/_ref/ref_solver_gpu.cubin,
